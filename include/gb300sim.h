@@ -1,0 +1,208 @@
+/*
+ * gb300sim.h — C ABI of the GB300 (sm_103a) state-vector simulator core.
+ *
+ * The library libgb300sim.so is a drop-in for the native engine behind
+ * ProjectQ's Python backend `projectq.backends.Simulator`, i.e. the pybind11
+ * class `projectq.backends._sim._cppsim.Simulator` bound in
+ * projectq/backends/_sim/_cppsim.cpp:45-66 and implemented in
+ * projectq/backends/_sim/_cppkernels/simulator.hpp:37-575.  Each entry point
+ * below names the reference method it replaces (file:line).
+ *
+ * Conventions
+ *  - Every function returns an int status: GSIM_OK (0) or one of the GSIM_ERR_*
+ *    codes.  The message of the last failure on the calling thread is returned
+ *    by gsim_last_error().  The codes mirror the C++ exception classes the
+ *    reference throws and pybind11 translates:
+ *      std::runtime_error    -> GSIM_ERR_RUNTIME -> Python RuntimeError
+ *      std::invalid_argument -> GSIM_ERR_VALUE   -> Python ValueError
+ *      std::length_error     -> GSIM_ERR_LENGTH  -> Python ValueError
+ *  - Qubits are named by caller-chosen 32-bit ids.  The engine keeps the
+ *    id -> bit-position map (simulator.hpp:42,567); the i-th allocated qubit
+ *    takes bit position i (simulator.hpp:57).
+ *  - Matrices are 2^k x 2^k complex128, row-major, interleaved (re, im):
+ *    2 * 4^k doubles.  Matrix bit l corresponds to ids[l] (ids[0] = LSB),
+ *    as in the reference kernels (fusion.hpp:79-100).
+ *  - Pauli terms are passed in CSR form: term t owns the factors
+ *    [term_offsets[t], term_offsets[t+1]) of op_qubit[] (an index into ids[])
+ *    and op_pauli[] (the characters 'X', 'Y', 'Z').  This is the reference's
+ *    Term = vector<pair<unsigned, char>> (simulator.hpp:44-46).
+ *  - All state lives in device memory of the current CUDA device.  Calls are
+ *    asynchronous on the engine's own stream except where a host result is
+ *    returned.  An engine is not thread-safe (as in the reference).
+ */
+#ifndef GB300SIM_H_
+#define GB300SIM_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GSIM_OK 0
+#define GSIM_ERR_RUNTIME 1
+#define GSIM_ERR_VALUE 2
+#define GSIM_ERR_LENGTH 3
+#define GSIM_ERR_CUDA 4
+#define GSIM_ERR_MEMORY 5
+
+/* Storage precision of the state vector. */
+#define GSIM_C128 0 /* complex128: the plain method, same arithmetic as the reference */
+#define GSIM_C64 1  /* complex64 storage, FP64 reductions */
+
+/* Fusion planners (the reference has exactly one: GSIM_FUSION_REFERENCE). */
+#define GSIM_FUSION_REFERENCE 0 /* simulator.hpp:204-222 + fusion.hpp, window 4..5 */
+#define GSIM_FUSION_NONE 1      /* every gate is its own pass */
+#define GSIM_FUSION_STAGED 2    /* shared-memory tiles: many gates per HBM pass */
+
+#if defined(__GNUC__)
+#define GSIM_API __attribute__((visibility("default")))
+#else
+#define GSIM_API
+#endif
+
+typedef struct gsim_engine gsim_engine;
+
+/* Message of the last failed call on this thread ("" if none). */
+GSIM_API const char *gsim_last_error(void);
+
+/* Number of CUDA devices visible (0 when no GPU); never fails. */
+GSIM_API int gsim_device_count(void);
+
+/* Simulator(seed) — simulator.hpp:48-53 (_cppsim.cpp:46).  precision is
+ * GSIM_C128 or GSIM_C64.  The RNG is std::mt19937(seed) feeding
+ * std::uniform_real_distribution<double>(0, 1), as in the reference. */
+GSIM_API int gsim_create(uint32_t seed, int precision, gsim_engine **out);
+
+/* ~Simulator — simulator.hpp:534-535.  Frees all device memory of the engine. */
+GSIM_API int gsim_destroy(gsim_engine *e);
+
+/* allocate_qubit — simulator.hpp:55-74.  The new qubit is the new top bit. */
+GSIM_API int gsim_allocate_qubit(gsim_engine *e, uint32_t id);
+
+/* deallocate_qubit — simulator.hpp:194-202.  RUNTIME error if not classical. */
+GSIM_API int gsim_deallocate_qubit(gsim_engine *e, uint32_t id);
+
+/* get_classical_value — simulator.hpp:76-91. */
+GSIM_API int gsim_get_classical_value(gsim_engine *e, uint32_t id, double tol, int *out);
+
+/* is_classical — simulator.hpp:93-108. */
+GSIM_API int gsim_is_classical(gsim_engine *e, uint32_t id, double tol, int *out);
+
+/* measure_qubits / measure_qubits_return — simulator.hpp:145-192.  One draw
+ * of the engine RNG per call; out[i] in {0,1}. */
+GSIM_API int gsim_measure_qubits(gsim_engine *e, const uint32_t *ids, size_t n, uint8_t *out);
+
+/* measure_qubits with the uniform draw supplied by the caller instead of the
+ * engine RNG (same sampling rule, simulator.hpp:152-160), for parity checks
+ * "at a given draw". */
+GSIM_API int gsim_measure_qubits_at(gsim_engine *e, const uint32_t *ids, size_t n, double rnd,
+                           uint8_t *out);
+
+/* apply_controlled_gate — simulator.hpp:204-222 (fusion: fusion.hpp:56-63). */
+GSIM_API int gsim_apply_controlled_gate(gsim_engine *e, const double *m, uint32_t k,
+                               const uint32_t *ids, const uint32_t *ctrl, size_t nctrl);
+
+/* run — simulator.hpp:487-527: apply every pending gate.  VALUE error for a
+ * fused gate wider than the engine's maximum (5, as in simulator.hpp:522). */
+GSIM_API int gsim_run(gsim_engine *e);
+
+/* emulate_math_addConstant — simulator.hpp:272-276.  Registers are given as
+ * reg_ids (all registers concatenated) and reg_sizes[nregs]. */
+GSIM_API int gsim_emulate_math_add_constant(gsim_engine *e, int32_t a, const uint32_t *reg_ids,
+                                   const uint32_t *reg_sizes, size_t nregs,
+                                   const uint32_t *ctrl, size_t nctrl);
+
+/* emulate_math_addConstantModN — simulator.hpp:279-283. */
+GSIM_API int gsim_emulate_math_add_constant_modn(gsim_engine *e, int32_t a, int32_t N,
+                                        const uint32_t *reg_ids, const uint32_t *reg_sizes,
+                                        size_t nregs, const uint32_t *ctrl, size_t nctrl);
+
+/* emulate_math_multiplyByConstantModN — simulator.hpp:286-290. */
+GSIM_API int gsim_emulate_math_multiply_by_constant_modn(gsim_engine *e, int32_t a, int32_t N,
+                                                const uint32_t *reg_ids,
+                                                const uint32_t *reg_sizes, size_t nregs,
+                                                const uint32_t *ctrl, size_t nctrl);
+
+/* emulate_math with a caller function — simulator.hpp:224-269 and
+ * _cppsim.cpp:33-41.  Instead of one callback per basis state, the caller
+ * tabulates the function once: table[x] is the packed output for the packed
+ * register input x (register 0 in the lowest reg_sizes[0] bits, and so on),
+ * for all 2^W inputs, W = sum(reg_sizes) <= 26. */
+GSIM_API int gsim_emulate_math_table(gsim_engine *e, const uint64_t *table, const uint32_t *reg_ids,
+                            const uint32_t *reg_sizes, size_t nregs, const uint32_t *ctrl,
+                            size_t nctrl);
+
+/* get_expectation_value — simulator.hpp:292-322 (+ apply_term :538-550).
+ * Real coefficients, as the reference's TermsDict (simulator.hpp:45). */
+GSIM_API int gsim_get_expectation_value(gsim_engine *e, const uint32_t *term_offsets,
+                               const uint32_t *op_qubit, const uint8_t *op_pauli,
+                               const double *coeffs, size_t nterms, const uint32_t *ids,
+                               size_t nids, double *out);
+
+/* apply_qubit_operator — simulator.hpp:324-350.  Complex coefficients,
+ * interleaved (re, im): 2 * nterms doubles. */
+GSIM_API int gsim_apply_qubit_operator(gsim_engine *e, const uint32_t *term_offsets,
+                              const uint32_t *op_qubit, const uint8_t *op_pauli,
+                              const double *coeffs, size_t nterms, const uint32_t *ids,
+                              size_t nids);
+
+/* emulate_time_evolution — simulator.hpp:386-438.  Real coefficients. */
+GSIM_API int gsim_emulate_time_evolution(gsim_engine *e, const uint32_t *term_offsets,
+                                const uint32_t *op_qubit, const uint8_t *op_pauli,
+                                const double *coeffs, size_t nterms, double time,
+                                const uint32_t *ids, size_t nids, const uint32_t *ctrl,
+                                size_t nctrl);
+
+/* get_probability — simulator.hpp:352-368.  bits[i] in {0,1}. */
+GSIM_API int gsim_get_probability(gsim_engine *e, const uint8_t *bits, const uint32_t *ids, size_t n,
+                         double *out);
+
+/* get_amplitude — simulator.hpp:370-384.  out = (re, im). */
+GSIM_API int gsim_get_amplitude(gsim_engine *e, const uint8_t *bits, const uint32_t *ids, size_t n,
+                       double *out);
+
+/* set_wavefunction — simulator.hpp:440-454.  wf holds len complex values of
+ * dtype GSIM_C128 (interleaved doubles) or GSIM_C64 (interleaved floats),
+ * in host memory. */
+GSIM_API int gsim_set_wavefunction(gsim_engine *e, const void *wf, int dtype, size_t len,
+                          const uint32_t *ordering, size_t n);
+
+/* collapse_wavefunction — simulator.hpp:456-485.  values[i] in {0,1}. */
+GSIM_API int gsim_collapse_wavefunction(gsim_engine *e, const uint32_t *ids, size_t n,
+                               const uint8_t *values, size_t nvalues);
+
+/* cheat — simulator.hpp:529-532, split in three calls so that no Python list
+ * of 2^N objects is built: the map (gsim_num_qubits + gsim_get_mapping) and a
+ * copy of [offset, offset+count) of the state into host memory as dtype. */
+GSIM_API int gsim_num_qubits(gsim_engine *e, uint32_t *out);
+GSIM_API int gsim_get_mapping(gsim_engine *e, uint32_t *ids, uint32_t *positions, size_t cap);
+GSIM_API int gsim_get_state(gsim_engine *e, void *host, int dtype, size_t offset, size_t count);
+
+/* Zero-copy view of the flushed device state (no reference counterpart; the
+ * reference returns a list copy, _cppsim.cpp:65).  Valid until the next call
+ * that changes the qubit count. */
+GSIM_API int gsim_state_device_ptr(gsim_engine *e, void **ptr, size_t *len, int *dtype);
+
+/* Wait for all work queued on the engine's stream. */
+GSIM_API int gsim_synchronize(gsim_engine *e);
+
+/* Select the fusion planner (GSIM_FUSION_*) and its widest fused gate. */
+GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
+
+/* Preallocate device memory for nqubits qubits (avoids regrowth). */
+GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
+
+/* Counters since creation or the last reset:
+ *  out[0] logical gates submitted, out[1] kernel launches for gates,
+ *  out[2] algorithmic bytes moved by gate kernels (2 x touched amplitudes
+ *  x bytes per amplitude), out[3] gate passes over the state. */
+GSIM_API int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n);
+GSIM_API int gsim_reset_counters(gsim_engine *e);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GB300SIM_H_ */

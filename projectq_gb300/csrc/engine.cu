@@ -1,0 +1,1118 @@
+// GB300 state-vector engine: host logic and the C ABI of include/gb300sim.h.
+//
+// The engine owns one state vector in device memory (complex128 or
+// complex64), the qubit-id -> bit-position map, the pending-gate queue and
+// one CUDA stream.  Every method mirrors a method of the reference engine
+// (projectq/backends/_sim/_cppkernels/simulator.hpp), cited at each one; the
+// data paths are GB300 kernels (kernels_gate.cu, kernels_state.cu).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstring>
+#include <map>
+#include <random>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/gb300sim.h"
+#include "fusion.hpp"
+#include "kernels.hpp"
+#include "stage.hpp"
+
+namespace gsim {
+
+struct Error {
+  int code;
+  std::string msg;
+};
+[[noreturn]] void fail(int code, const std::string &m) { throw Error{code, m}; }
+
+#define CK(x)                                                                        \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess)                                                           \
+      fail(GSIM_ERR_CUDA, std::string("CUDA error: ") + cudaGetErrorString(e_) +     \
+                              " (" #x ")");                                          \
+  } while (0)
+
+thread_local std::string g_last_error;
+
+// Device buffer that grows on demand (never shrinks until the engine dies).
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  void *get(size_t need) {
+    if (need > bytes) {
+      if (p) CK(cudaFree(p));
+      p = nullptr;
+      bytes = 0;
+      if (cudaMalloc(&p, need) != cudaSuccess) {
+        cudaGetLastError();
+        fail(GSIM_ERR_MEMORY, "cudaMalloc of " + std::to_string(need) + " bytes failed");
+      }
+      bytes = need;
+    }
+    return p;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+struct HostBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+  void *get(size_t need) {
+    if (need > bytes) {
+      if (p) cudaFreeHost(p);
+      p = nullptr;
+      bytes = 0;
+      if (cudaMallocHost(&p, need) != cudaSuccess) {
+        cudaGetLastError();
+        fail(GSIM_ERR_MEMORY, "cudaMallocHost failed");
+      }
+      bytes = need;
+    }
+    return p;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+};
+
+struct PauliTerm {
+  uint64_t xmask = 0, sign_mask = 0;
+  int ny = 0;          // phase (-i)^ny
+  bool empty = false;  // no factors: the identity term of simulator.hpp:394-395
+};
+
+class Engine {
+ public:
+  Engine(uint32_t seed, int prec) : prec_(prec), bpa_(prec == GSIM_C64 ? 8 : 16), rng_(seed) {
+    if (prec != GSIM_C64 && prec != GSIM_C128) fail(GSIM_ERR_VALUE, "unknown precision");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      fail(GSIM_ERR_CUDA, "no CUDA device available");
+    }
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    ensure_capacity(0);
+    set_basis_zero();
+  }
+  ~Engine() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (DevBuf *b : {&state_, &scratch_, &part_, &small_, &aux1_, &aux2_, &aux3_, &table_, &table2_})
+      b->release();
+    pinned_.release();
+    if (stream_) cudaStreamDestroy(stream_);
+  }
+
+  // ---- simulator.hpp:55-74 ------------------------------------------------
+  void allocate_qubit(unsigned id) {
+    if (map_.count(id))
+      fail(GSIM_ERR_RUNTIME, "AllocateQubit: ID already exists. Qubit IDs should be unique.");
+    if (N_ >= 40) fail(GSIM_ERR_MEMORY, "too many qubits");
+    ensure_capacity(N_ + 1);
+    const size_t half = size_t(1) << N_;
+    CK(cudaMemsetAsync(static_cast<char *>(state_.p) + half * bpa_, 0, half * bpa_, stream_));
+    map_[id] = N_++;
+  }
+
+  // ---- simulator.hpp:194-202 ----------------------------------------------
+  void deallocate_qubit(unsigned id) {
+    run();
+    const unsigned pos = pos_of(id);
+    if (!is_classical(id, 1e-12))
+      fail(GSIM_ERR_RUNTIME,
+           "Error: Qubit has not been measured / uncomputed! There is most likely a bug in your "
+           "code.");
+    const bool value = get_classical_value(id, 1e-12);
+    // collapse_vector(id, value, shrink=true), simulator.hpp:110-143.
+    if (pos == N_ - 1) {
+      if (value) {
+        const size_t half = size_t(1) << (N_ - 1);
+        CK(cudaMemcpyAsync(state_.p, static_cast<char *>(state_.p) + half * bpa_, half * bpa_,
+                           cudaMemcpyDeviceToDevice, stream_));
+      }
+    } else {
+      void *dst = scratch();
+      CK(launch_shrink(prec_, state_.p, dst, N_, pos, value ? 1 : 0, stream_));
+      std::swap(state_, scratch_);
+    }
+    for (auto &p : map_)
+      if (p.second > pos) p.second--;
+    map_.erase(id);
+    N_--;
+  }
+
+  // ---- simulator.hpp:76-91 ------------------------------------------------
+  bool get_classical_value(unsigned id, double tol) {
+    run();
+    const unsigned pos = pos_of(id);
+    if (N_ == 0) return false;
+    auto *d_first = static_cast<unsigned long long *>(small_.get(4096));
+    CK(cudaMemsetAsync(d_first, 0xff, sizeof(unsigned long long), stream_));
+    CK(launch_classical_first(prec_, state_.p, N_, pos, tol, d_first, stream_));
+    unsigned long long first = 0;
+    CK(cudaMemcpyAsync(&first, d_first, sizeof(first), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (first == ~0ull) return false;  // unreachable for a normalised state
+    const uint64_t lo = ((first >> pos) << (pos + 1)) | (first & ((uint64_t(1) << pos) - 1));
+    return !(norm2_at(lo) > tol);
+  }
+
+  // ---- simulator.hpp:93-108 -----------------------------------------------
+  bool is_classical(unsigned id, double tol) {
+    run();
+    const unsigned pos = pos_of(id);
+    if (N_ == 0) return false;
+    int *d_flags = static_cast<int *>(small_.get(4096));
+    CK(cudaMemsetAsync(d_flags, 0, 2 * sizeof(int), stream_));
+    CK(launch_classical_flags(prec_, state_.p, N_, pos, tol, d_flags, stream_));
+    int f[2];
+    CK(cudaMemcpyAsync(f, d_flags, sizeof(f), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return 1 == (f[0] ^ f[1]);
+  }
+
+  // ---- simulator.hpp:145-186 ----------------------------------------------
+  std::vector<uint8_t> measure(const std::vector<unsigned> &ids, bool have_rnd, double rnd) {
+    run();
+    std::vector<unsigned> positions(ids.size());
+    for (size_t i = 0; i < ids.size(); ++i) positions[i] = pos_of(ids[i]);
+    if (!have_rnd) rnd = dist_(rng_);
+    const uint64_t pick = sample(rnd);
+    std::vector<uint8_t> res(ids.size());
+    uint64_t mask = 0, val = 0;
+    for (size_t i = 0; i < ids.size(); ++i) {
+      const bool r = ((pick >> positions[i]) & 1) == 1;
+      res[i] = r;
+      mask |= uint64_t(1) << positions[i];
+      val |= uint64_t(r) << positions[i];
+    }
+    double *d_norm = static_cast<double *>(small_.get(4096));
+    CK(launch_masked_norm(prec_, state_.p, N_, mask, val, part(), d_norm, stream_));
+    CK(launch_project_scale(prec_, state_.p, N_, mask, val, d_norm, stream_));
+    return res;
+  }
+
+  // ---- simulator.hpp:204-222 ----------------------------------------------
+  void apply_controlled_gate(std::vector<cplx> m, const std::vector<unsigned> &ids,
+                             const std::vector<unsigned> &ctrl) {
+    if (ids.empty()) fail(GSIM_ERR_VALUE, "apply_controlled_gate(): a gate needs target qubits");
+    std::set<unsigned> seen;
+    for (unsigned q : ids) {
+      pos_of(q);
+      if (!seen.insert(q).second) fail(GSIM_ERR_VALUE, "apply_controlled_gate(): repeated target qubit");
+    }
+    for (unsigned q : ctrl) {
+      pos_of(q);
+      if (!seen.insert(q).second)
+        fail(GSIM_ERR_VALUE, "apply_controlled_gate(): a control is also a target or repeated");
+    }
+    counters_[0] += 1;
+    if (mode_ == GSIM_FUSION_STAGED) {
+      queue_.push_back(QueuedGate{std::move(m), ids, ctrl});
+      if (queue_.size() >= kMaxQueue) run();
+      return;
+    }
+    if (mode_ == GSIM_FUSION_NONE) {
+      fused_.insert(std::move(m), ids, ctrl);
+      run();
+      return;
+    }
+    RefFusion f = fused_;
+    f.insert(m, ids, ctrl);
+    const unsigned nf = f.num_qubits();
+    if (nf >= fmin_ && nf <= fmax_) {
+      fused_ = std::move(f);
+      run();
+    } else if (nf > fmax_ || (nf - unsigned(ids.size())) > fused_.num_qubits()) {
+      run();
+      fused_.insert(std::move(m), ids, ctrl);
+    } else {
+      fused_ = std::move(f);
+    }
+  }
+
+  // ---- simulator.hpp:487-527 ----------------------------------------------
+  void run() {
+    if (mode_ == GSIM_FUSION_STAGED) {
+      run_staged();
+      return;
+    }
+    if (fused_.size() < 1) return;
+    std::vector<cplx> M;
+    std::vector<unsigned> ids, ctrls;
+    fused_.compose(M, ids, ctrls);
+    if (ids.size() > max_gate_)
+      fail(GSIM_ERR_VALUE, "Gates with more than " + std::to_string(max_gate_) +
+                               " qubits are not supported!");
+    DenseOp op;
+    op.m = std::move(M);
+    for (unsigned q : ids) op.pos.push_back(pos_of(q));
+    for (unsigned c : ctrls) op.ctrl_mask |= uint64_t(1) << pos_of(c);
+    fused_ = RefFusion();
+    exec_dense(op);
+  }
+
+  // ---- simulator.hpp:224-290 ----------------------------------------------
+  // f maps the packed register value to the packed result (per-register
+  // results already truncated to their widths).
+  template <class F>
+  void emulate_math(F const &f, const std::vector<unsigned> &reg_ids,
+                    const std::vector<unsigned> &reg_sizes, const std::vector<unsigned> &ctrl) {
+    run();
+    uint64_t cm = 0;
+    for (unsigned c : ctrl) cm |= uint64_t(1) << pos_of(c);
+    MathRegsDev R;
+    std::memset(&R, 0, sizeof(R));
+    unsigned W = 0;
+    for (unsigned s : reg_sizes) W += s;
+    if (W != reg_ids.size()) fail(GSIM_ERR_VALUE, "emulate_math(): register sizes do not match ids");
+    if (W > 26) fail(GSIM_ERR_VALUE, "emulate_math(): at most 26 register qubits are supported");
+    uint64_t used = 0;
+    for (unsigned b = 0; b < W; ++b) {
+      const unsigned p = pos_of(reg_ids[b]);
+      if ((used >> p) & 1) fail(GSIM_ERR_VALUE, "emulate_math(): repeated register qubit");
+      if ((cm >> p) & 1) fail(GSIM_ERR_VALUE, "emulate_math(): a control qubit is in a register");
+      used |= uint64_t(1) << p;
+      R.pos[b] = uint8_t(p);
+    }
+    R.width = int(W);
+    R.ctrl = cm;
+    const size_t T = size_t(1) << W;
+    std::vector<uint32_t> table(T);
+    std::vector<uint32_t> count(T, 0);
+    for (size_t x = 0; x < T; ++x) {
+      table[x] = uint32_t(f(uint64_t(x)) & (T - 1));
+      count[table[x]]++;
+    }
+    bool bijective = true;
+    for (size_t y = 0; y < T && bijective; ++y) bijective = count[y] == 1;
+    void *dst = scratch();
+    if (bijective) {
+      auto *d_table = static_cast<uint32_t *>(table_.get(T * 4));
+      CK(cudaMemcpyAsync(d_table, table.data(), T * 4, cudaMemcpyHostToDevice, stream_));
+      CK(launch_math_scatter(prec_, state_.p, dst, N_, R, d_table, stream_));
+    } else {
+      // Inverse lists, each sorted by the sources' bit pattern in the state
+      // index: the reference accumulates colliding amplitudes in index order.
+      std::vector<uint64_t> off(T + 1, 0);
+      for (size_t y = 0; y < T; ++y) off[y + 1] = off[y] + count[y];
+      std::vector<uint32_t> src(T);
+      std::vector<uint64_t> fill(off.begin(), off.end() - 1);
+      std::vector<uint32_t> order(T);
+      for (size_t x = 0; x < T; ++x) order[x] = uint32_t(x);
+      auto key = [&](uint32_t x) {
+        uint64_t k = 0;
+        for (unsigned b = 0; b < W; ++b) k |= uint64_t((x >> b) & 1) << R.pos[b];
+        return k;
+      };
+      std::sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return key(a) < key(b); });
+      for (uint32_t x : order) src[fill[table[x]]++] = x;
+      auto *d_off = static_cast<uint64_t *>(table_.get((T + 1) * 8));
+      auto *d_src = static_cast<uint32_t *>(table2_.get(T * 4));
+      CK(cudaMemcpyAsync(d_off, off.data(), (T + 1) * 8, cudaMemcpyHostToDevice, stream_));
+      CK(cudaMemcpyAsync(d_src, src.data(), T * 4, cudaMemcpyHostToDevice, stream_));
+      CK(launch_math_gather(prec_, state_.p, dst, N_, R, d_off, d_src, stream_));
+    }
+    std::swap(state_, scratch_);
+    // The host tables must outlive the asynchronous copies.
+    CK(cudaStreamSynchronize(stream_));
+  }
+
+  // ---- simulator.hpp:292-322 ----------------------------------------------
+  double get_expectation_value(const std::vector<PauliTerm> &terms, const std::vector<double> &coeffs) {
+    run();
+    const int nt = int(terms.size());
+    if (nt == 0) return 0.;
+    const int nblk = pauli_expect_blocks(N_);
+    double *d_part = static_cast<double *>(aux1_.get(size_t(nt) * nblk * 8));
+    double *d_out = static_cast<double *>(aux2_.get(size_t(nt) * 8));
+    // Group terms by flip mask: one read pass of the state per group.
+    std::map<uint64_t, std::vector<int>> groups;
+    for (int t = 0; t < nt; ++t) groups[terms[t].xmask].push_back(t);
+    // Columns are laid out group by group; remember each term's column.
+    std::vector<int> col(nt);
+    int c0 = 0;
+    for (auto const &g : groups) {
+      std::vector<PauliTermDev> dev;
+      for (int t : g.second) {
+        col[t] = c0 + int(dev.size());
+        dev.push_back(PauliTermDev{terms[t].sign_mask, terms[t].ny & 3, 0});
+      }
+      CK(launch_pauli_expect(prec_, state_.p, N_, g.first, dev.data(), int(dev.size()),
+                             d_part + size_t(c0) * nblk, nblk, stream_));
+      c0 += int(dev.size());
+    }
+    CK(launch_column_sums(d_part, nblk, nt, d_out, stream_));
+    std::vector<double> delta(nt);
+    CK(cudaMemcpyAsync(delta.data(), d_out, nt * 8, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    double e = 0.;
+    for (int t = 0; t < nt; ++t) e += coeffs[t] * delta[col[t]];
+    return e;
+  }
+
+  // ---- simulator.hpp:324-350 ----------------------------------------------
+  void apply_qubit_operator(const std::vector<PauliTerm> &terms, const std::vector<cplx> &coeffs) {
+    run();
+    std::vector<PauliApplyTermDev> dev(terms.size());
+    for (size_t t = 0; t < terms.size(); ++t) dev[t] = apply_term_dev(terms[t], coeffs[t]);
+    auto *d_terms = static_cast<PauliApplyTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliApplyTermDev)));
+    if (!dev.empty())
+      CK(cudaMemcpyAsync(d_terms, dev.data(), dev.size() * sizeof(dev[0]), cudaMemcpyHostToDevice, stream_));
+    void *dst = scratch();
+    CK(launch_pauli_apply(prec_, state_.p, dst, N_, d_terms, int(dev.size()), stream_));
+    std::swap(state_, scratch_);
+    CK(cudaStreamSynchronize(stream_));
+  }
+
+  // ---- simulator.hpp:386-438 ----------------------------------------------
+  void emulate_time_evolution(const std::vector<PauliTerm> &terms, const std::vector<double> &coeffs,
+                              double time, const std::vector<unsigned> &ctrl) {
+    run();
+    uint64_t cm = 0;
+    for (unsigned c : ctrl) cm |= uint64_t(1) << pos_of(c);
+    double tr = 0., op_nrm = 0.;
+    std::vector<PauliApplyTermDev> dev;
+    for (size_t t = 0; t < terms.size(); ++t) {
+      if (terms[t].empty) {
+        tr += coeffs[t];
+      } else {
+        dev.push_back(apply_term_dev(terms[t], cplx(coeffs[t], 0.)));
+        op_nrm += std::abs(coeffs[t]);
+      }
+    }
+    const unsigned s = unsigned(std::abs(time) * op_nrm + 1.);
+    const cplx I(0., 1.);
+    const cplx corr = std::exp(-time * I * tr / double(s));
+    const size_t n = size_t(1) << N_;
+    auto *vec = static_cast<double2 *>(aux1_.get(n * 16));
+    auto *nxt = static_cast<double2 *>(aux2_.get(n * 16));
+    auto *out = static_cast<double2 *>(scratch_c128(n));
+    CK(launch_convert(0, vec, prec_ == GSIM_C64 ? 1 : 0, state_.p, n, stream_));
+    CK(cudaMemcpyAsync(out, vec, n * 16, cudaMemcpyDeviceToDevice, stream_));
+    auto *d_terms = static_cast<PauliApplyTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliApplyTermDev)));
+    if (!dev.empty())
+      CK(cudaMemcpyAsync(d_terms, dev.data(), dev.size() * sizeof(dev[0]), cudaMemcpyHostToDevice, stream_));
+    double *d_norm = static_cast<double *>(small_.get(4096));
+    for (unsigned i = 0; i < s; ++i) {
+      double nrm_change = 1.;
+      for (unsigned k = 0; nrm_change > 1.e-12; ++k) {
+        const cplx coeff = (-time * I) / double(s * (k + 1));
+        CK(launch_taylor_step(vec, nxt, out, N_, d_terms, int(dev.size()), coeff.real(), coeff.imag(),
+                              cm, part(), d_norm, stream_));
+        std::swap(vec, nxt);
+        double h = 0.;
+        CK(cudaMemcpyAsync(&h, d_norm, 8, cudaMemcpyDeviceToHost, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        nrm_change = std::sqrt(h);
+        if (k > 100000) fail(GSIM_ERR_RUNTIME, "emulate_time_evolution(): Taylor series did not converge");
+      }
+      CK(launch_phase_ctrl(out, vec, n, cm, corr.real(), corr.imag(), stream_));
+    }
+    CK(launch_convert(prec_ == GSIM_C64 ? 1 : 0, state_.p, 0, out, n, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    // aux1_/aux2_ hold two full complex128 vectors: give the memory back.
+    aux1_.release();
+    aux2_.release();
+  }
+
+  // ---- simulator.hpp:352-368 ----------------------------------------------
+  double get_probability(const std::vector<uint8_t> &bits, const std::vector<unsigned> &ids) {
+    run();
+    if (!check_ids(ids))
+      fail(GSIM_ERR_RUNTIME,
+           "get_probability(): Unknown qubit id. Please make sure you have called eng.flush().");
+    if (bits.size() != ids.size()) fail(GSIM_ERR_LENGTH, "get_probability(): bits and ids size mismatch");
+    uint64_t mask = 0, val = 0;
+    for (size_t i = 0; i < ids.size(); ++i) {
+      mask |= uint64_t(1) << map_.at(ids[i]);
+      val |= uint64_t(bits[i] ? 1 : 0) << map_.at(ids[i]);
+    }
+    return masked_norm_host(mask, val);
+  }
+
+  // ---- simulator.hpp:370-384 ----------------------------------------------
+  cplx get_amplitude(const std::vector<uint8_t> &bits, const std::vector<unsigned> &ids) {
+    run();
+    uint64_t chk = 0, index = 0;
+    for (size_t i = 0; i < ids.size(); ++i) {
+      auto it = map_.find(ids[i]);
+      if (it == map_.end()) break;
+      chk |= uint64_t(1) << it->second;
+      index |= uint64_t(i < bits.size() && bits[i] ? 1 : 0) << it->second;
+    }
+    if (chk + 1 != (uint64_t(1) << N_))
+      fail(GSIM_ERR_RUNTIME,
+           "The second argument to get_amplitude() must be a permutation of all allocated qubits. "
+           "Please make sure you have called eng.flush().");
+    return amp_at(index);
+  }
+
+  // ---- simulator.hpp:440-454 ----------------------------------------------
+  void set_wavefunction(const void *wf, int dtype, size_t len, const std::vector<unsigned> &ordering) {
+    run();
+    if (map_.size() != ordering.size() || !check_ids(ordering))
+      fail(GSIM_ERR_RUNTIME,
+           "set_wavefunction(): Invalid mapping provided. Please make sure all qubits have been "
+           "allocated previously (call eng.flush()).");
+    if (len != (size_t(1) << ordering.size()))
+      fail(GSIM_ERR_LENGTH, "set_wavefunction(): the wavefunction must have 2^n amplitudes");
+    if (dtype != GSIM_C64 && dtype != GSIM_C128) fail(GSIM_ERR_VALUE, "unknown dtype");
+    for (size_t i = 0; i < ordering.size(); ++i) map_[ordering[i]] = unsigned(i);
+    upload(wf, dtype, 0, len);
+  }
+
+  // ---- simulator.hpp:456-485 ----------------------------------------------
+  void collapse_wavefunction(const std::vector<unsigned> &ids, const std::vector<uint8_t> &values) {
+    run();
+    if (ids.size() != values.size())
+      fail(GSIM_ERR_LENGTH, "collapse_wavefunction(): ids and values size mismatch");
+    if (!check_ids(ids))
+      fail(GSIM_ERR_RUNTIME,
+           "collapse_wavefunction(): Unknown qubit id(s) provided. Try calling eng.flush() before "
+           "invoking this function.");
+    uint64_t mask = 0, val = 0;
+    for (size_t i = 0; i < ids.size(); ++i) {
+      mask |= uint64_t(1) << map_.at(ids[i]);
+      val |= uint64_t(values[i] ? 1 : 0) << map_.at(ids[i]);
+    }
+    double *d_norm = static_cast<double *>(small_.get(4096));
+    CK(launch_masked_norm(prec_, state_.p, N_, mask, val, part(), d_norm, stream_));
+    double nrm = 0.;
+    CK(cudaMemcpyAsync(&nrm, d_norm, 8, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    if (nrm < 1.e-12)
+      fail(GSIM_ERR_RUNTIME, "collapse_wavefunction(): Invalid collapse! Probability is ~0.");
+    CK(launch_project_scale(prec_, state_.p, N_, mask, val, d_norm, stream_));
+  }
+
+  // ---- cheat, simulator.hpp:529-532 ---------------------------------------
+  unsigned num_qubits() {
+    run();
+    return N_;
+  }
+  const std::map<unsigned, unsigned> &mapping() const { return map_; }
+  void get_state(void *host, int dtype, size_t offset, size_t count) {
+    run();
+    if (offset + count > (size_t(1) << N_)) fail(GSIM_ERR_LENGTH, "state range out of bounds");
+    if (dtype != GSIM_C64 && dtype != GSIM_C128) fail(GSIM_ERR_VALUE, "unknown dtype");
+    download(host, dtype, offset, count);
+  }
+  void device_view(void **ptr, size_t *len, int *dtype) {
+    run();
+    CK(cudaStreamSynchronize(stream_));
+    *ptr = state_.p;
+    *len = size_t(1) << N_;
+    *dtype = prec_;
+  }
+  void synchronize() { CK(cudaStreamSynchronize(stream_)); }
+
+  void set_fusion(int mode, unsigned kmax) {
+    run();
+    if (mode != GSIM_FUSION_REFERENCE && mode != GSIM_FUSION_NONE && mode != GSIM_FUSION_STAGED)
+      fail(GSIM_ERR_VALUE, "unknown fusion mode");
+    mode_ = mode;
+    if (kmax) kmax_ = std::min(kmax, 5u);
+  }
+  void reserve(unsigned nq) { ensure_capacity(nq); }
+  uint64_t counter(size_t i) const { return i < 4 ? counters_[i] : 0; }
+  void reset_counters() { std::fill(std::begin(counters_), std::end(counters_), 0); }
+
+ private:
+  struct QueuedGate {
+    std::vector<cplx> m;
+    std::vector<unsigned> ids, ctrl;
+  };
+  static constexpr size_t kMaxQueue = 4096;
+
+  unsigned pos_of(unsigned id) const {
+    auto it = map_.find(id);
+    if (it == map_.end())
+      fail(GSIM_ERR_RUNTIME, "Unknown qubit id " + std::to_string(id) +
+                                 ". Please make sure you have called eng.flush().");
+    return it->second;
+  }
+  bool check_ids(const std::vector<unsigned> &ids) const {
+    for (unsigned id : ids)
+      if (!map_.count(id)) return false;
+    return true;
+  }
+
+  PauliApplyTermDev apply_term_dev(const PauliTerm &t, cplx c) const {
+    // (P psi)_i = (-i)^{#Y} (-1)^{popcount(i & (Y|Z))} psi_{i ^ X}.
+    static const cplx ph[4] = {cplx(1, 0), cplx(0, -1), cplx(-1, 0), cplx(0, 1)};
+    const cplx w = c * ph[t.ny & 3];
+    return PauliApplyTermDev{t.xmask, t.sign_mask, w.real(), w.imag()};
+  }
+
+  double *part() { return static_cast<double *>(part_.get(4096 * 8)); }
+  void *scratch() { return scratch_.get(cap_ * bpa_); }
+  void *scratch_c128(size_t n) {
+    // emulate_time_evolution's third complex128 vector: reuse the scratch
+    // buffer when it is large enough.
+    return scratch_.get(std::max(cap_ * bpa_, n * 16));
+  }
+
+  void ensure_capacity(unsigned nq) {
+    const size_t need = size_t(1) << std::max(nq, 10u);
+    if (need <= cap_) return;
+    void *np = nullptr;
+    if (cudaMalloc(&np, need * bpa_) != cudaSuccess) {
+      cudaGetLastError();
+      fail(GSIM_ERR_MEMORY, "cudaMalloc of the state vector (" + std::to_string(need * bpa_) +
+                                " bytes) failed");
+    }
+    if (state_.p) {
+      CK(cudaMemcpyAsync(np, state_.p, (size_t(1) << N_) * bpa_, cudaMemcpyDeviceToDevice, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      state_.release();
+    }
+    state_.p = np;
+    state_.bytes = need * bpa_;
+    cap_ = need;
+    scratch_.release();  // regrown on demand at the new capacity
+  }
+  void set_basis_zero() {
+    CK(cudaMemsetAsync(state_.p, 0, bpa_, stream_));
+    if (prec_ == GSIM_C64) {
+      const float one[2] = {1.f, 0.f};
+      CK(cudaMemcpyAsync(state_.p, one, 8, cudaMemcpyHostToDevice, stream_));
+    } else {
+      const double one[2] = {1., 0.};
+      CK(cudaMemcpyAsync(state_.p, one, 16, cudaMemcpyHostToDevice, stream_));
+    }
+    CK(cudaStreamSynchronize(stream_));
+  }
+
+  void exec_dense(const DenseOp &op) {
+    CK(launch_dense(prec_, state_.p, N_, op, stream_));
+    const unsigned c = unsigned(__builtin_popcountll(op.ctrl_mask));
+    counters_[1] += 1;
+    counters_[2] += 2 * (uint64_t(1) << (N_ - c)) * bpa_;
+    counters_[3] += 1;
+  }
+
+  void run_staged();
+
+  double masked_norm_host(uint64_t mask, uint64_t val) {
+    double *d_norm = static_cast<double *>(small_.get(4096));
+    CK(launch_masked_norm(prec_, state_.p, N_, mask, val, part(), d_norm, stream_));
+    double h = 0.;
+    CK(cudaMemcpyAsync(&h, d_norm, 8, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return h;
+  }
+  cplx amp_at(uint64_t index) {
+    if (prec_ == GSIM_C64) {
+      float a[2];
+      CK(cudaMemcpyAsync(a, static_cast<char *>(state_.p) + index * 8, 8, cudaMemcpyDeviceToHost, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      return cplx(a[0], a[1]);
+    }
+    double a[2];
+    CK(cudaMemcpyAsync(a, static_cast<char *>(state_.p) + index * 16, 16, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return cplx(a[0], a[1]);
+  }
+  static double norm2_host(double re, double im) { return std::fma(re, re, im * im); }
+  double norm2_at(uint64_t index) {
+    const cplx a = amp_at(index);
+    return norm2_host(a.real(), a.imag());
+  }
+
+  // Host <-> device transfers with precision conversion through the scratch
+  // buffer, in chunks.
+  void upload(const void *host, int dtype, size_t offset, size_t count) {
+    const size_t hb = dtype == GSIM_C64 ? 8 : 16;
+    if (dtype == prec_) {
+      CK(cudaMemcpyAsync(static_cast<char *>(state_.p) + offset * bpa_, host, count * bpa_,
+                         cudaMemcpyHostToDevice, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      return;
+    }
+    char *stage = static_cast<char *>(scratch());
+    const size_t chunk = std::max<size_t>(1, (cap_ * bpa_) / hb);
+    for (size_t o = 0; o < count; o += chunk) {
+      const size_t c = std::min(chunk, count - o);
+      CK(cudaMemcpyAsync(stage, static_cast<const char *>(host) + o * hb, c * hb, cudaMemcpyHostToDevice, stream_));
+      CK(launch_convert(prec_ == GSIM_C64 ? 1 : 0, static_cast<char *>(state_.p) + (offset + o) * bpa_,
+                        dtype == GSIM_C64 ? 1 : 0, stage, c, stream_));
+      CK(cudaStreamSynchronize(stream_));
+    }
+  }
+  void download(void *host, int dtype, size_t offset, size_t count) {
+    const size_t hb = dtype == GSIM_C64 ? 8 : 16;
+    if (dtype == prec_) {
+      CK(cudaMemcpyAsync(host, static_cast<char *>(state_.p) + offset * bpa_, count * bpa_,
+                         cudaMemcpyDeviceToHost, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      return;
+    }
+    char *stage = static_cast<char *>(scratch());
+    const size_t chunk = std::max<size_t>(1, (cap_ * bpa_) / hb);
+    for (size_t o = 0; o < count; o += chunk) {
+      const size_t c = std::min(chunk, count - o);
+      CK(launch_convert(dtype == GSIM_C64 ? 1 : 0, stage, prec_ == GSIM_C64 ? 1 : 0,
+                        static_cast<char *>(state_.p) + (offset + o) * bpa_, c, stream_));
+      CK(cudaMemcpyAsync(static_cast<char *>(host) + o * hb, stage, c * hb, cudaMemcpyDeviceToHost, stream_));
+      CK(cudaStreamSynchronize(stream_));
+    }
+  }
+
+  // Index picked by the reference's sampling loop (simulator.hpp:152-160):
+  //   P = 0; pick = 0; while (P < rnd && pick < n) P += |psi[pick++]|^2; pick--;
+  // reproduced exactly, including FP64 rounding of the running sum.
+  uint64_t sample(double rnd);
+  double seq_block(uint64_t b0, uint64_t cnt, double P, double rnd, uint64_t &pick, bool &done);
+
+  int prec_;
+  size_t bpa_;
+  unsigned N_ = 0;
+  std::map<unsigned, unsigned> map_;
+  DevBuf state_, scratch_, part_, small_, aux1_, aux2_, aux3_, table_, table2_;
+  HostBuf pinned_;
+  size_t cap_ = 0;
+  cudaStream_t stream_ = nullptr;
+  std::mt19937 rng_;
+  std::uniform_real_distribution<double> dist_{0., 1.};
+  RefFusion fused_;
+  unsigned fmin_ = 4, fmax_ = 5, max_gate_ = 5, kmax_ = 5;
+  int mode_ = GSIM_FUSION_REFERENCE;
+  std::vector<QueuedGate> queue_;
+  uint64_t counters_[4] = {0, 0, 0, 0};
+};
+
+// Sequential reference loop over [b0, b0 + cnt) starting from running sum P.
+double Engine::seq_block(uint64_t b0, uint64_t cnt, double P, double rnd, uint64_t &pick,
+                         bool &done) {
+  char *h = static_cast<char *>(pinned_.get(cnt * bpa_));
+  CK(cudaMemcpyAsync(h, static_cast<char *>(state_.p) + b0 * bpa_, cnt * bpa_, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  for (uint64_t i = 0; i < cnt; ++i) {
+    if (!(P < rnd)) {
+      done = true;
+      return P;
+    }
+    double re, im;
+    if (prec_ == GSIM_C64) {
+      re = reinterpret_cast<float *>(h)[2 * i];
+      im = reinterpret_cast<float *>(h)[2 * i + 1];
+    } else {
+      re = reinterpret_cast<double *>(h)[2 * i];
+      im = reinterpret_cast<double *>(h)[2 * i + 1];
+    }
+    P += norm2_host(re, im);
+    pick = b0 + i + 1;
+  }
+  return P;
+}
+
+uint64_t Engine::sample(double rnd) {
+  const uint64_t n = uint64_t(1) << N_;
+  uint64_t pick = 0;
+  bool done = false;
+  if (!(0. < rnd)) return ~uint64_t(0);  // loop never runs: pick-- wraps
+  constexpr unsigned lb = 13;
+  if (n <= (uint64_t(1) << 16)) {
+    seq_block(0, n, 0., rnd, pick, done);
+    return pick - 1;
+  }
+  // Blocked exact replay.  Within a block where the running sum P stays in
+  // one binade [2^e, 2^(e+1)), every addition rounds to the grid 2^(e-52),
+  // so fl(P + x) = P + round(x) unless x sits exactly half-way between grid
+  // points.  Block sums of round(x) are exact 64-bit integers computed in
+  // parallel for three candidate binades per block; the host replays the
+  // blocks in order and falls back to the element loop for a block that
+  // changes binade, holds a tie, or reaches rnd.
+  const uint64_t B = n >> lb;
+  auto *d_sums = static_cast<double *>(aux1_.get(B * 8));
+  CK(launch_block_norm_sums(prec_, state_.p, n, lb, d_sums, stream_));
+  std::vector<double> sums(B);
+  CK(cudaMemcpyAsync(sums.data(), d_sums, B * 8, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  std::vector<int16_t> cand(3 * B);
+  double Q = 0.;
+  for (uint64_t b = 0; b < B; ++b) {
+    if (Q > 0. && std::isfinite(Q)) {
+      const int e = std::ilogb(Q);
+      for (int c = 0; c < 3; ++c) cand[3 * b + c] = int16_t(e - 1 + c);
+    } else {
+      for (int c = 0; c < 3; ++c) cand[3 * b + c] = int16_t(-32768);
+    }
+    Q += sums[b];
+  }
+  auto *d_cand = static_cast<int16_t *>(aux2_.get(3 * B * 2 + 3 * B * 8 + 3 * B + 64));
+  auto *d_units = reinterpret_cast<unsigned long long *>(
+      reinterpret_cast<char *>(d_cand) + ((3 * B * 2 + 15) / 16) * 16);
+  auto *d_flags = reinterpret_cast<uint8_t *>(d_units + 3 * B);
+  CK(cudaMemcpyAsync(d_cand, cand.data(), 3 * B * 2, cudaMemcpyHostToDevice, stream_));
+  CK(launch_block_grid_sums(prec_, state_.p, n, lb, d_cand, d_units, d_flags, stream_));
+  std::vector<unsigned long long> units(3 * B);
+  std::vector<uint8_t> flags(3 * B);
+  CK(cudaMemcpyAsync(units.data(), d_units, 3 * B * 8, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaMemcpyAsync(flags.data(), d_flags, 3 * B, cudaMemcpyDeviceToHost, stream_));
+  CK(cudaStreamSynchronize(stream_));
+  double P = 0.;
+  const uint64_t bsz = uint64_t(1) << lb;
+  for (uint64_t b = 0; b < B && !done; ++b) {
+    const uint64_t b0 = b * bsz;
+    if (P == 0.) {
+      if (sums[b] == 0.) {
+        pick = b0 + bsz;  // every x in the block is 0: P stays 0 < rnd
+        continue;
+      }
+      P = seq_block(b0, bsz, P, rnd, pick, done);
+      continue;
+    }
+    const int e = std::ilogb(P);
+    int c = -1;
+    for (int k = 0; k < 3; ++k)
+      if (cand[3 * b + k] == e) c = k;
+    bool fast = c >= 0 && flags[3 * b + c] == 0 && e > -1000;
+    if (fast) {
+      const double G = std::ldexp(1., e - 52);
+      const unsigned long long p = (unsigned long long)(P / G);  // exact: P is a multiple of G
+      const unsigned long long S = units[3 * b + c];
+      if (p + S < (1ull << 53)) {
+        const double Pn = double(p + S) * G;
+        if (Pn < rnd) {
+          P = Pn;
+          pick = b0 + bsz;
+          continue;
+        }
+      }
+    }
+    P = seq_block(b0, bsz, P, rnd, pick, done);
+  }
+  return pick - 1;
+}
+
+void Engine::run_staged() {
+  if (queue_.empty()) return;
+  std::vector<QueuedGate> q;
+  q.swap(queue_);
+  // Plan stages over the queue; each stage is one pass over the state.
+  std::vector<StageGate> gates;
+  gates.reserve(q.size());
+  for (auto &g : q) {
+    StageGate sg;
+    sg.m = std::move(g.m);
+    for (unsigned id : g.ids) sg.pos.push_back(pos_of(id));
+    for (unsigned c : g.ctrl) sg.ctrl_mask |= uint64_t(1) << pos_of(c);
+    gates.push_back(std::move(sg));
+  }
+  StagePlanner planner(N_, prec_, kmax_);
+  std::vector<DenseOp> ops = planner.fuse(gates);
+  for (auto const &op : ops) exec_dense(op);
+}
+
+}  // namespace gsim
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using gsim::Engine;
+using gsim::Error;
+
+namespace {
+template <class F>
+int guard(F &&f) {
+  try {
+    f();
+    return GSIM_OK;
+  } catch (const Error &e) {
+    gsim::g_last_error = e.msg;
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    gsim::g_last_error = "out of host memory";
+    return GSIM_ERR_MEMORY;
+  } catch (const std::invalid_argument &e) {
+    gsim::g_last_error = e.what();
+    return GSIM_ERR_VALUE;
+  } catch (const std::exception &e) {
+    gsim::g_last_error = e.what();
+    return GSIM_ERR_RUNTIME;
+  }
+}
+Engine *E(gsim_engine *e) {
+  if (!e) gsim::fail(GSIM_ERR_VALUE, "null engine handle");
+  return reinterpret_cast<Engine *>(e);
+}
+std::vector<unsigned> vu(const uint32_t *p, size_t n) {
+  return n ? std::vector<unsigned>(p, p + n) : std::vector<unsigned>();
+}
+std::vector<unsigned> reg_sizes(const uint32_t *s, size_t n) { return vu(s, n); }
+
+// Pauli terms in CSR form -> engine terms (positions resolved through ids).
+// A term's factors are applied in order, as apply_term does through the gate
+// path (simulator.hpp:538-550), so the product is F_last ... F_first.  It is
+// kept as i^k X^x Z^z (per qubit X^{x_q} Z^{z_q}); Y = i X Z, and moving a new
+// factor's Z past an existing X costs a sign.  Then
+//   (X^x Z^z psi)_i = (-1)^{popcount(x & z)} (-1)^{popcount(i & z)} psi_{i ^ x},
+// and the kernels use P psi = (-i)^{ny} (-1)^{popcount(i & z)} psi_{i ^ x}.
+std::vector<gsim::PauliTerm> terms_of(Engine *eng, const uint32_t *off, const uint32_t *q,
+                                      const uint8_t *pa, size_t nterms, const uint32_t *ids,
+                                      size_t nids) {
+  const std::map<unsigned, unsigned> &m = eng->mapping();
+  std::vector<gsim::PauliTerm> out(nterms);
+  for (size_t t = 0; t < nterms; ++t) {
+    gsim::PauliTerm pt;
+    pt.empty = off[t + 1] == off[t];
+    int k = 0;
+    for (uint32_t f = off[t]; f < off[t + 1]; ++f) {
+      if (q[f] >= nids) gsim::fail(GSIM_ERR_VALUE, "Pauli term acts on a qubit index outside the qureg");
+      auto it = m.find(ids[q[f]]);
+      if (it == m.end())
+        gsim::fail(GSIM_ERR_RUNTIME, "Unknown qubit id. Please make sure you have called eng.flush().");
+      const uint64_t bit = uint64_t(1) << it->second;
+      const char c = char(pa[f]);
+      if (c != 'X' && c != 'Y' && c != 'Z') gsim::fail(GSIM_ERR_VALUE, "Pauli must be X, Y or Z");
+      const bool fx = c == 'X' || c == 'Y', fz = c == 'Z' || c == 'Y';
+      if (c == 'Y') k += 1;
+      if (fz && (pt.xmask & bit)) k += 2;
+      if (fx) pt.xmask ^= bit;
+      if (fz) pt.sign_mask ^= bit;
+    }
+    const int ipow = (k + 2 * (__builtin_popcountll(pt.xmask & pt.sign_mask) & 1)) & 3;
+    pt.ny = (4 - ipow) & 3;  // (-i)^ny == i^ipow
+    out[t] = pt;
+  }
+  return out;
+}
+std::vector<unsigned> reg_shift(const uint32_t *sizes, size_t nregs) {
+  std::vector<unsigned> sh(nregs, 0);
+  for (size_t r = 1; r < nregs; ++r) sh[r] = sh[r - 1] + sizes[r - 1];
+  return sh;
+}
+// Per-register function on 32-bit ints, as the reference's lambdas
+// (simulator.hpp:275,282,289); results are truncated to the register width.
+template <class F>
+int math_fast(gsim_engine *e, F f, const uint32_t *reg_ids, const uint32_t *sizes,
+                     size_t nregs, const uint32_t *ctrl, size_t nctrl) {
+  return guard([&] {
+    size_t W = 0;
+    for (size_t r = 0; r < nregs; ++r) W += sizes[r];
+    auto sh = reg_shift(sizes, nregs);
+    auto g = [&](uint64_t x) {
+      uint64_t y = 0;
+      for (size_t r = 0; r < nregs; ++r) {
+        const uint64_t mask = (uint64_t(1) << sizes[r]) - 1;
+        const int v = int((x >> sh[r]) & mask);
+        const int res = f(v);
+        y |= (uint64_t(uint32_t(res)) & mask) << sh[r];
+      }
+      return y;
+    };
+    E(e)->emulate_math(g, vu(reg_ids, W), reg_sizes(sizes, nregs), vu(ctrl, nctrl));
+  });
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gsim_last_error(void) { return gsim::g_last_error.c_str(); }
+
+int gsim_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int gsim_create(uint32_t seed, int precision, gsim_engine **out) {
+  return guard([&] {
+    if (!out) gsim::fail(GSIM_ERR_VALUE, "null output pointer");
+    *out = reinterpret_cast<gsim_engine *>(new Engine(seed, precision));
+  });
+}
+int gsim_destroy(gsim_engine *e) {
+  return guard([&] { delete reinterpret_cast<Engine *>(e); });
+}
+int gsim_allocate_qubit(gsim_engine *e, uint32_t id) {
+  return guard([&] { E(e)->allocate_qubit(id); });
+}
+int gsim_deallocate_qubit(gsim_engine *e, uint32_t id) {
+  return guard([&] { E(e)->deallocate_qubit(id); });
+}
+int gsim_get_classical_value(gsim_engine *e, uint32_t id, double tol, int *out) {
+  return guard([&] { *out = E(e)->get_classical_value(id, tol) ? 1 : 0; });
+}
+int gsim_is_classical(gsim_engine *e, uint32_t id, double tol, int *out) {
+  return guard([&] { *out = E(e)->is_classical(id, tol) ? 1 : 0; });
+}
+int gsim_measure_qubits(gsim_engine *e, const uint32_t *ids, size_t n, uint8_t *out) {
+  return guard([&] {
+    auto r = E(e)->measure(vu(ids, n), false, 0.);
+    std::copy(r.begin(), r.end(), out);
+  });
+}
+int gsim_measure_qubits_at(gsim_engine *e, const uint32_t *ids, size_t n, double rnd, uint8_t *out) {
+  return guard([&] {
+    auto r = E(e)->measure(vu(ids, n), true, rnd);
+    std::copy(r.begin(), r.end(), out);
+  });
+}
+int gsim_apply_controlled_gate(gsim_engine *e, const double *m, uint32_t k, const uint32_t *ids,
+                               const uint32_t *ctrl, size_t nctrl) {
+  return guard([&] {
+    if (k == 0 || k > 16) gsim::fail(GSIM_ERR_VALUE, "apply_controlled_gate(): bad gate width");
+    const size_t d = size_t(1) << k;
+    std::vector<gsim::cplx> M(d * d);
+    for (size_t i = 0; i < d * d; ++i) M[i] = gsim::cplx(m[2 * i], m[2 * i + 1]);
+    E(e)->apply_controlled_gate(std::move(M), vu(ids, k), vu(ctrl, nctrl));
+  });
+}
+int gsim_run(gsim_engine *e) {
+  return guard([&] { E(e)->run(); });
+}
+
+int gsim_emulate_math_add_constant(gsim_engine *e, int32_t a, const uint32_t *reg_ids,
+                                   const uint32_t *reg_sizes_, size_t nregs, const uint32_t *ctrl,
+                                   size_t nctrl) {
+  return math_fast(e, [a](int x) { return int(uint32_t(x) + uint32_t(a)); }, reg_ids, reg_sizes_,
+                   nregs, ctrl, nctrl);
+}
+int gsim_emulate_math_add_constant_modn(gsim_engine *e, int32_t a, int32_t N, const uint32_t *reg_ids,
+                                        const uint32_t *reg_sizes_, size_t nregs,
+                                        const uint32_t *ctrl, size_t nctrl) {
+  if (N == 0) {
+    gsim::g_last_error = "modulus N must be nonzero";
+    return GSIM_ERR_VALUE;
+  }
+  return math_fast(e, [a, N](int x) { return int(uint32_t(x) + uint32_t(a)) % N; }, reg_ids,
+                   reg_sizes_, nregs, ctrl, nctrl);
+}
+int gsim_emulate_math_multiply_by_constant_modn(gsim_engine *e, int32_t a, int32_t N,
+                                                const uint32_t *reg_ids, const uint32_t *reg_sizes_,
+                                                size_t nregs, const uint32_t *ctrl, size_t nctrl) {
+  if (N == 0) {
+    gsim::g_last_error = "modulus N must be nonzero";
+    return GSIM_ERR_VALUE;
+  }
+  return math_fast(e, [a, N](int x) { return int(uint32_t(x) * uint32_t(a)) % N; }, reg_ids,
+                   reg_sizes_, nregs, ctrl, nctrl);
+}
+int gsim_emulate_math_table(gsim_engine *e, const uint64_t *table, const uint32_t *reg_ids,
+                            const uint32_t *sizes, size_t nregs, const uint32_t *ctrl, size_t nctrl) {
+  return guard([&] {
+    size_t W = 0;
+    for (size_t r = 0; r < nregs; ++r) W += sizes[r];
+    if (W > 26) gsim::fail(GSIM_ERR_VALUE, "emulate_math(): at most 26 register qubits are supported");
+    auto sh = reg_shift(sizes, nregs);
+    auto g = [&](uint64_t x) {
+      const uint64_t y = table[x];
+      uint64_t r = 0;
+      for (size_t k = 0; k < nregs; ++k) {
+        const uint64_t mask = (uint64_t(1) << sizes[k]) - 1;
+        r |= ((y >> sh[k]) & mask) << sh[k];
+      }
+      return r;
+    };
+    E(e)->emulate_math(g, vu(reg_ids, W), reg_sizes(sizes, nregs), vu(ctrl, nctrl));
+  });
+}
+
+int gsim_get_expectation_value(gsim_engine *e, const uint32_t *off, const uint32_t *q,
+                               const uint8_t *pa, const double *coeffs, size_t nterms,
+                               const uint32_t *ids, size_t nids, double *out) {
+  return guard([&] {
+    Engine *eng = E(e);
+    eng->run();
+    auto terms = terms_of(eng, off, q, pa, nterms, ids, nids);
+    *out = eng->get_expectation_value(terms, std::vector<double>(coeffs, coeffs + nterms));
+  });
+}
+int gsim_apply_qubit_operator(gsim_engine *e, const uint32_t *off, const uint32_t *q,
+                              const uint8_t *pa, const double *coeffs, size_t nterms,
+                              const uint32_t *ids, size_t nids) {
+  return guard([&] {
+    Engine *eng = E(e);
+    eng->run();
+    auto terms = terms_of(eng, off, q, pa, nterms, ids, nids);
+    std::vector<gsim::cplx> c(nterms);
+    for (size_t t = 0; t < nterms; ++t) c[t] = gsim::cplx(coeffs[2 * t], coeffs[2 * t + 1]);
+    eng->apply_qubit_operator(terms, c);
+  });
+}
+int gsim_emulate_time_evolution(gsim_engine *e, const uint32_t *off, const uint32_t *q,
+                                const uint8_t *pa, const double *coeffs, size_t nterms, double time,
+                                const uint32_t *ids, size_t nids, const uint32_t *ctrl, size_t nctrl) {
+  return guard([&] {
+    Engine *eng = E(e);
+    eng->run();
+    auto terms = terms_of(eng, off, q, pa, nterms, ids, nids);
+    eng->emulate_time_evolution(terms, std::vector<double>(coeffs, coeffs + nterms), time, vu(ctrl, nctrl));
+  });
+}
+int gsim_get_probability(gsim_engine *e, const uint8_t *bits, const uint32_t *ids, size_t n, double *out) {
+  return guard([&] { *out = E(e)->get_probability(std::vector<uint8_t>(bits, bits + n), vu(ids, n)); });
+}
+int gsim_get_amplitude(gsim_engine *e, const uint8_t *bits, const uint32_t *ids, size_t n, double *out) {
+  return guard([&] {
+    auto a = E(e)->get_amplitude(std::vector<uint8_t>(bits, bits + n), vu(ids, n));
+    out[0] = a.real();
+    out[1] = a.imag();
+  });
+}
+int gsim_set_wavefunction(gsim_engine *e, const void *wf, int dtype, size_t len, const uint32_t *ordering,
+                          size_t n) {
+  return guard([&] { E(e)->set_wavefunction(wf, dtype, len, vu(ordering, n)); });
+}
+int gsim_collapse_wavefunction(gsim_engine *e, const uint32_t *ids, size_t n, const uint8_t *values,
+                               size_t nvalues) {
+  return guard([&] {
+    E(e)->collapse_wavefunction(vu(ids, n), std::vector<uint8_t>(values, values + nvalues));
+  });
+}
+int gsim_num_qubits(gsim_engine *e, uint32_t *out) {
+  return guard([&] { *out = E(e)->num_qubits(); });
+}
+int gsim_get_mapping(gsim_engine *e, uint32_t *ids, uint32_t *positions, size_t cap) {
+  return guard([&] {
+    size_t i = 0;
+    for (auto const &p : E(e)->mapping()) {
+      if (i >= cap) break;
+      ids[i] = p.first;
+      positions[i] = p.second;
+      ++i;
+    }
+  });
+}
+int gsim_get_state(gsim_engine *e, void *host, int dtype, size_t offset, size_t count) {
+  return guard([&] { E(e)->get_state(host, dtype, offset, count); });
+}
+int gsim_state_device_ptr(gsim_engine *e, void **ptr, size_t *len, int *dtype) {
+  return guard([&] { E(e)->device_view(ptr, len, dtype); });
+}
+int gsim_synchronize(gsim_engine *e) {
+  return guard([&] { E(e)->synchronize(); });
+}
+int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax) {
+  return guard([&] { E(e)->set_fusion(mode, kmax); });
+}
+int gsim_reserve(gsim_engine *e, uint32_t nqubits) {
+  return guard([&] { E(e)->reserve(nqubits); });
+}
+int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n) {
+  return guard([&] {
+    for (size_t i = 0; i < n; ++i) out[i] = E(e)->counter(i);
+  });
+}
+int gsim_reset_counters(gsim_engine *e) {
+  return guard([&] { E(e)->reset_counters(); });
+}
+
+}  // extern "C"

@@ -1,0 +1,114 @@
+// Host-side declarations of the CUDA kernels' launchers.  Plain C++: the
+// engine (engine.cu) plans the work, these functions enqueue it on a stream.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <vector>
+
+namespace gsim {
+
+using cplx = std::complex<double>;
+
+// One controlled dense k-qubit gate on bit positions pos[] (matrix bit l is
+// pos[l]); the gate acts where (index & ctrl_mask) == ctrl_mask.
+struct DenseOp {
+  std::vector<cplx> m;        // 2^k x 2^k, row-major, FP64
+  std::vector<unsigned> pos;  // k distinct bit positions
+  uint64_t ctrl_mask = 0;
+};
+
+// prec: 0 = complex128 state, 1 = complex64 state.
+cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s);
+
+// ---- stage kernel (many gates per pass through shared-memory tiles) -----
+struct StagePlan;  // defined in stage.hpp
+cudaError_t launch_stage(int prec, void *psi, unsigned nq, const StagePlan &plan,
+                         const void *d_ops, cudaStream_t s);
+
+// ---- reductions and state kernels (kernels_state.cu) ---------------------
+// Sum over indices i with (i & mask) == val of |psi_i|^2 (FP64 accumulation).
+// Writes the result to *d_out (device).  d_part: >= 4096 doubles of scratch.
+cudaError_t launch_masked_norm(int prec, const void *psi, unsigned nq, uint64_t mask,
+                               uint64_t val, double *d_part, double *d_out, cudaStream_t s);
+
+// psi_i <- 0 where (i & mask) != val, psi_i <- psi_i / sqrt(*d_norm) otherwise.
+cudaError_t launch_project_scale(int prec, void *psi, unsigned nq, uint64_t mask, uint64_t val,
+                                 const double *d_norm, cudaStream_t s);
+
+// d_flags[0] |= any |psi_i|^2 > tol with bit pos = 0; d_flags[1] likewise for bit = 1.
+cudaError_t launch_classical_flags(int prec, const void *psi, unsigned nq, unsigned pos,
+                                   double tol, int *d_flags, cudaStream_t s);
+// d_first = min pair index p (bit pos removed) where either side exceeds tol.
+cudaError_t launch_classical_first(int prec, const void *psi, unsigned nq, unsigned pos,
+                                   double tol, unsigned long long *d_first, cudaStream_t s);
+
+// dst <- src with bit `pos` removed, keeping the half where that bit == value.
+cudaError_t launch_shrink(int prec, const void *src, void *dst, unsigned nq, unsigned pos,
+                          int value, cudaStream_t s);
+
+// Measurement sampling support (see measure.cu).
+cudaError_t launch_block_norm_sums(int prec, const void *psi, uint64_t n, unsigned log_block,
+                                   double *d_sums, cudaStream_t s);
+cudaError_t launch_block_grid_sums(int prec, const void *psi, uint64_t n, unsigned log_block,
+                                   const int16_t *d_cand, unsigned long long *d_units,
+                                   uint8_t *d_flags, cudaStream_t s);
+
+// Convert between storage precisions: dst_prec/src_prec 0 = c128, 1 = c64.
+cudaError_t launch_convert(int dst_prec, void *dst, int src_prec, const void *src, uint64_t n,
+                           cudaStream_t s);
+
+// Pauli strings.  For one group of terms that share the flip mask x:
+// part[t * nblk + b] = per-block partial of Re<psi| P_t |psi> / coefficient.
+struct PauliTermDev {
+  uint64_t sign_mask;  // Y|Z positions: sign (-1)^popcount(i & sign_mask)
+  int32_t phase;       // number of Y factors mod 4 (phase (-i)^phase)
+  int32_t pad;
+};
+cudaError_t launch_pauli_expect(int prec, const void *psi, unsigned nq, uint64_t xmask,
+                                const PauliTermDev *d_terms, int nterms, double *d_part,
+                                int nblk, cudaStream_t s);
+int pauli_expect_blocks(unsigned nq);
+// Column sums: out[c] = sum_b part[c * nblk + b], fixed order.
+cudaError_t launch_column_sums(const double *d_part, int nblk, int ncols, double *d_out,
+                               cudaStream_t s);
+
+// out_i = sum_t coeff_t (P_t in)_i for a list of terms (complex coefficients).
+struct PauliApplyTermDev {
+  uint64_t xmask;
+  uint64_t sign_mask;
+  double cre, cim;  // coefficient times (-i)^{#Y}
+};
+cudaError_t launch_pauli_apply(int prec, const void *in, void *out, unsigned nq,
+                               const PauliApplyTermDev *d_terms, int nterms, cudaStream_t s);
+
+// One Taylor order of emulate_time_evolution, all FP64 (complex128 vectors):
+//   upd_j = coeff * sum_t c_t (P_t vec)_j ; vec_next_j = upd_j ;
+//   where (j & ctrl) == ctrl: out_j += upd_j and part += |upd_j|^2.
+cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *out, unsigned nq,
+                               const PauliApplyTermDev *d_terms, int nterms, double coeff_re,
+                               double coeff_im, uint64_t ctrl, double *d_part, double *d_norm,
+                               cudaStream_t s);
+// out_j *= corr where (j & ctrl) == ctrl; vec_j = out_j.
+cudaError_t launch_phase_ctrl(double2 *out, double2 *vec, uint64_t n, uint64_t ctrl, double cre,
+                              double cim, cudaStream_t s);
+
+// emulate_math: out_j = sum over sources s of in_s, gathered through an
+// inverse table (CSR) over the packed register value, in the reference's
+// accumulation order; uncontrolled indices are copied.
+struct MathRegsDev {
+  uint8_t pos[64];  // bit positions of the packed register value, LSB first
+  int width;        // total number of register bits W
+  uint64_t ctrl;    // control mask
+};
+cudaError_t launch_math_gather(int prec, const void *in, void *out, unsigned nq,
+                               const MathRegsDev &regs, const uint64_t *d_inv_off,
+                               const uint32_t *d_inv_src, cudaStream_t s);
+// Bijective case: out[deposit(j, table[x])] = in[j] + 0.0 (a scatter).
+cudaError_t launch_math_scatter(int prec, const void *in, void *out, unsigned nq,
+                                const MathRegsDev &regs, const uint32_t *d_table,
+                                cudaStream_t s);
+
+}  // namespace gsim

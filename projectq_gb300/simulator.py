@@ -1,0 +1,355 @@
+"""Python face of the GB300 engine: a drop-in for ProjectQ's native simulator.
+
+`Simulator` has the method surface of the pybind11 class
+``projectq.backends._sim._cppsim.Simulator`` (projectq/backends/_sim/
+_cppsim.cpp:45-66): same names, same argument meaning, same return types and
+the same exception classes (RuntimeError / ValueError / TypeError).  Plug it
+into ProjectQ's Python backend exactly as the reference's tests do
+(projectq/backends/_sim/_simulator_test.py:80-93)::
+
+    from projectq.backends import Simulator
+    from projectq_gb300 import Simulator as GB300Simulator
+    sim = Simulator(gate_fusion=True)
+    sim._simulator = GB300Simulator(seed)
+
+Every method goes through the C ABI of include/gb300sim.h into
+libgb300sim.so; there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import numbers
+
+import numpy as np
+
+from . import _lib
+
+_PRECISIONS = {"c128": _lib.GSIM_C128, "complex128": _lib.GSIM_C128, "c64": _lib.GSIM_C64,
+               "complex64": _lib.GSIM_C64}
+_FUSION = {"reference": _lib.GSIM_FUSION_REFERENCE, "none": _lib.GSIM_FUSION_NONE,
+           "staged": _lib.GSIM_FUSION_STAGED}
+
+
+def _u32(seq) -> np.ndarray:
+    return np.ascontiguousarray(np.asarray(seq, dtype=np.int64).astype(np.uint32, copy=False)
+                                if len(seq) else np.zeros(0, dtype=np.uint32))
+
+
+def _p(arr: np.ndarray, ctype):
+    return arr.ctypes.data_as(C.POINTER(ctype))
+
+
+def _bits(bits) -> np.ndarray:
+    return np.ascontiguousarray([1 if bool(b) else 0 for b in bits], dtype=np.uint8)
+
+
+def _ids(ids) -> list:
+    out = []
+    for i in ids:
+        if isinstance(i, bool) or not isinstance(i, numbers.Integral):
+            raise TypeError("qubit ids must be integers")
+        if i < 0 or i > 0xFFFFFFFF:
+            raise TypeError("qubit ids must fit in an unsigned 32-bit integer")
+        out.append(int(i))
+    return out
+
+
+def _real(c):
+    """A real coefficient, or TypeError as pybind11's double caster raises."""
+    if isinstance(c, (complex, np.complexfloating)):
+        raise TypeError("incompatible function arguments: coefficient must be a real number")
+    return float(c)
+
+
+def _pauli_csr(terms, real: bool):
+    """[(term, coeff)] with term = [(index, 'X'|'Y'|'Z'), ...] -> CSR arrays."""
+    off = [0]
+    qs, ps, cs = [], [], []
+    for term, coeff in terms:
+        for idx, op in term:
+            op = op.decode() if isinstance(op, bytes) else op
+            if op not in ("X", "Y", "Z"):
+                raise ValueError(f"unknown Pauli operator {op!r}")
+            qs.append(int(idx))
+            ps.append(ord(op))
+        off.append(len(qs))
+        if real:
+            cs.append(_real(coeff))
+        else:
+            c = complex(coeff)
+            cs.extend([c.real, c.imag])
+    return (np.ascontiguousarray(off, dtype=np.uint32), _u32(qs),
+            np.ascontiguousarray(ps, dtype=np.uint8), np.ascontiguousarray(cs, dtype=np.float64))
+
+
+class Simulator:
+    """GB300 state-vector engine with the reference engine's method surface.
+
+    Args:
+        rnd_seed: seed of the engine's std::mt19937 (as the reference).
+        precision: "c128" (default; the plain method, FP64 like the reference)
+            or "c64" (complex64 storage with FP64 reductions).
+        fusion: gate-fusion planner: "reference" (default; the reference's
+            greedy 4..5-qubit rule), "none" or "staged".
+    """
+
+    def __init__(self, rnd_seed=1, *args, precision="c128", fusion="reference", _api=None, **kwargs):
+        if isinstance(rnd_seed, bool) or not isinstance(rnd_seed, numbers.Integral):
+            raise TypeError("Simulator(): seed must be an unsigned 32-bit integer")
+        if rnd_seed < 0 or rnd_seed > 0xFFFFFFFF:
+            raise TypeError("Simulator(): seed must be an unsigned 32-bit integer")
+        self._api = _api if _api is not None else _lib.load()
+        self._prec = _PRECISIONS[precision]
+        h = C.c_void_p()
+        self._check(self._api.create(int(rnd_seed), self._prec, C.byref(h)))
+        self._h = h
+        if fusion != "reference":
+            self.set_fusion(fusion)
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, rc):
+        _lib.check(self._api, rc)
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                self._api.destroy(h)
+            except Exception:  # pragma: no cover - interpreter shutdown
+                pass
+            self._h = None
+
+    @property
+    def precision(self) -> str:
+        return "c64" if self._prec == _lib.GSIM_C64 else "c128"
+
+    # -- the reference surface (_cppsim.cpp:45-66) ----------------------------
+    def allocate_qubit(self, qubit_id):
+        """simulator.hpp:55-74."""
+        (qid,) = _ids([qubit_id])
+        self._check(self._api.allocate_qubit(self._h, qid))
+
+    def deallocate_qubit(self, qubit_id):
+        """simulator.hpp:194-202."""
+        (qid,) = _ids([qubit_id])
+        self._check(self._api.deallocate_qubit(self._h, qid))
+
+    def get_classical_value(self, qubit_id, tol=1.0e-12):
+        """simulator.hpp:76-91."""
+        (qid,) = _ids([qubit_id])
+        out = C.c_int()
+        self._check(self._api.get_classical_value(self._h, qid, float(tol), C.byref(out)))
+        return bool(out.value)
+
+    def is_classical(self, qubit_id, tol=1.0e-12):
+        """simulator.hpp:93-108."""
+        (qid,) = _ids([qubit_id])
+        out = C.c_int()
+        self._check(self._api.is_classical(self._h, qid, float(tol), C.byref(out)))
+        return bool(out.value)
+
+    def measure_qubits(self, ids):
+        """simulator.hpp:145-192: one RNG draw; returns list[bool]."""
+        ids = _u32(_ids(ids))
+        out = np.zeros(len(ids), dtype=np.uint8)
+        self._check(self._api.measure_qubits(self._h, _p(ids, C.c_uint32), len(ids), _p(out, C.c_uint8)))
+        return [bool(v) for v in out]
+
+    def measure_qubits_at(self, ids, rnd):
+        """measure_qubits with the uniform draw `rnd` given instead of drawn."""
+        ids = _u32(_ids(ids))
+        out = np.zeros(len(ids), dtype=np.uint8)
+        self._check(self._api.measure_qubits_at(self._h, _p(ids, C.c_uint32), len(ids), float(rnd),
+                                                _p(out, C.c_uint8)))
+        return [bool(v) for v in out]
+
+    def apply_controlled_gate(self, m, ids, ctrl):
+        """simulator.hpp:204-222: queue a controlled gate (fused, run lazily)."""
+        ids = _ids(ids)
+        ctrl = _u32(_ids(ctrl))
+        mat = np.ascontiguousarray(m, dtype=np.complex128)
+        k = len(ids)
+        if mat.ndim != 2 or mat.shape != (1 << k, 1 << k):
+            raise ValueError(f"apply_controlled_gate(): a {k}-qubit gate needs a {1 << k}x{1 << k} matrix")
+        ida = _u32(ids)
+        self._check(self._api.apply_controlled_gate(self._h, _p(mat.view(np.float64), C.c_double), k,
+                                                    _p(ida, C.c_uint32), _p(ctrl, C.c_uint32), len(ctrl)))
+
+    def run(self):
+        """simulator.hpp:487-527: apply all pending gates."""
+        self._check(self._api.run(self._h))
+
+    def _regs(self, quregs):
+        sizes = [len(r) for r in quregs]
+        flat = [q for r in quregs for q in _ids(r)]
+        return _u32(flat), _u32(sizes), len(sizes)
+
+    def emulate_math(self, f, quregs, ctrl):
+        """simulator.hpp:224-269 with a Python function of the register values.
+
+        The reference calls `f` once per basis state (through the GIL,
+        _cppsim.cpp:33-41); here `f` is tabulated once over every tuple of
+        register values and the permutation runs on the GPU.
+        """
+        sizes = [len(r) for r in quregs]
+        W = sum(sizes)
+        if W > 26:
+            raise ValueError("emulate_math(): at most 26 register qubits are supported")
+        shifts = np.cumsum([0] + sizes[:-1]).tolist()
+        masks = [(1 << s) - 1 for s in sizes]
+        table = np.empty(1 << W, dtype=np.uint64)
+        for x in range(1 << W):
+            vals = [(x >> sh) & mk for sh, mk in zip(shifts, masks)]
+            res = f(vals)
+            y = 0
+            for r, (sh, mk) in enumerate(zip(shifts, masks)):
+                y |= (int(res[r]) & mk) << sh
+            table[x] = y
+        ids, sz, nr = self._regs(quregs)
+        ctrl = _u32(_ids(ctrl))
+        self._check(self._api.emulate_math_table(self._h, _p(table, C.c_uint64), _p(ids, C.c_uint32),
+                                                 _p(sz, C.c_uint32), nr, _p(ctrl, C.c_uint32), len(ctrl)))
+
+    def emulate_math_addConstant(self, a, quregs, ctrl):  # noqa: N802 (reference name)
+        """simulator.hpp:272-276."""
+        ids, sz, nr = self._regs(quregs)
+        ctrl = _u32(_ids(ctrl))
+        self._check(self._api.emulate_math_add_constant(self._h, int(a), _p(ids, C.c_uint32), _p(sz, C.c_uint32),
+                                                        nr, _p(ctrl, C.c_uint32), len(ctrl)))
+
+    def emulate_math_addConstantModN(self, a, N, quregs, ctrl):  # noqa: N802,N803
+        """simulator.hpp:279-283."""
+        ids, sz, nr = self._regs(quregs)
+        ctrl = _u32(_ids(ctrl))
+        self._check(self._api.emulate_math_add_constant_modn(self._h, int(a), int(N), _p(ids, C.c_uint32),
+                                                             _p(sz, C.c_uint32), nr, _p(ctrl, C.c_uint32),
+                                                             len(ctrl)))
+
+    def emulate_math_multiplyByConstantModN(self, a, N, quregs, ctrl):  # noqa: N802,N803
+        """simulator.hpp:286-290."""
+        ids, sz, nr = self._regs(quregs)
+        ctrl = _u32(_ids(ctrl))
+        self._check(self._api.emulate_math_multiply_by_constant_modn(
+            self._h, int(a), int(N), _p(ids, C.c_uint32), _p(sz, C.c_uint32), nr, _p(ctrl, C.c_uint32),
+            len(ctrl)))
+
+    def get_expectation_value(self, terms, ids):
+        """simulator.hpp:292-322: sum_t c_t <psi|P_t|psi> (real c_t)."""
+        off, q, pa, cs = _pauli_csr(terms, real=True)
+        ida = _u32(_ids(ids))
+        out = C.c_double()
+        self._check(self._api.get_expectation_value(self._h, _p(off, C.c_uint32), _p(q, C.c_uint32),
+                                                    _p(pa, C.c_uint8), _p(cs, C.c_double), len(off) - 1,
+                                                    _p(ida, C.c_uint32), len(ida), C.byref(out)))
+        return out.value
+
+    def apply_qubit_operator(self, terms, ids):
+        """simulator.hpp:324-350: psi <- sum_t c_t P_t psi (complex c_t)."""
+        off, q, pa, cs = _pauli_csr(terms, real=False)
+        ida = _u32(_ids(ids))
+        self._check(self._api.apply_qubit_operator(self._h, _p(off, C.c_uint32), _p(q, C.c_uint32),
+                                                   _p(pa, C.c_uint8), _p(cs, C.c_double), len(off) - 1,
+                                                   _p(ida, C.c_uint32), len(ida)))
+
+    def emulate_time_evolution(self, terms, time, ids, ctrl):
+        """simulator.hpp:386-438: exp(-i t H) by Taylor series (FP64)."""
+        off, q, pa, cs = _pauli_csr(terms, real=True)
+        ida = _u32(_ids(ids))
+        ctrl = _u32(_ids(ctrl))
+        self._check(self._api.emulate_time_evolution(self._h, _p(off, C.c_uint32), _p(q, C.c_uint32),
+                                                     _p(pa, C.c_uint8), _p(cs, C.c_double), len(off) - 1,
+                                                     float(time), _p(ida, C.c_uint32), len(ida),
+                                                     _p(ctrl, C.c_uint32), len(ctrl)))
+
+    def get_probability(self, bit_string, ids):
+        """simulator.hpp:352-368."""
+        bits = _bits(bit_string)
+        ida = _u32(_ids(ids))
+        out = C.c_double()
+        self._check(self._api.get_probability(self._h, _p(bits, C.c_uint8), _p(ida, C.c_uint32), len(ida),
+                                              C.byref(out)))
+        return out.value
+
+    def get_amplitude(self, bit_string, ids):
+        """simulator.hpp:370-384."""
+        bits = _bits(bit_string)
+        ida = _u32(_ids(ids))
+        if len(bits) < len(ida):
+            bits = np.concatenate([bits, np.zeros(len(ida) - len(bits), dtype=np.uint8)])
+        out = np.zeros(2, dtype=np.float64)
+        self._check(self._api.get_amplitude(self._h, _p(bits, C.c_uint8), _p(ida, C.c_uint32), len(ida),
+                                            _p(out, C.c_double)))
+        return complex(out[0], out[1])
+
+    def set_wavefunction(self, wavefunction, ordering):
+        """simulator.hpp:440-454."""
+        wf = np.asarray(wavefunction)
+        if wf.dtype == np.complex64:
+            dtype = _lib.GSIM_C64
+        else:
+            wf = wf.astype(np.complex128, copy=False)
+            dtype = _lib.GSIM_C128
+        wf = np.ascontiguousarray(wf.reshape(-1))
+        ordv = _u32(_ids(ordering))
+        self._check(self._api.set_wavefunction(self._h, wf.ctypes.data_as(C.c_void_p), dtype, wf.size,
+                                               _p(ordv, C.c_uint32), len(ordv)))
+
+    def collapse_wavefunction(self, ids, values):
+        """simulator.hpp:456-485."""
+        ida = _u32(_ids(ids))
+        vals = _bits(values)
+        self._check(self._api.collapse_wavefunction(self._h, _p(ida, C.c_uint32), len(ida), _p(vals, C.c_uint8),
+                                                    len(vals)))
+
+    def cheat(self, dtype=np.complex128):
+        """simulator.hpp:529-532: (qubit id -> bit position, state vector).
+
+        The state is a NumPy array (the reference returns a list copy).
+        """
+        n = C.c_uint32()
+        self._check(self._api.num_qubits(self._h, C.byref(n)))
+        nq = n.value
+        ids = np.zeros(max(nq, 1), dtype=np.uint32)
+        pos = np.zeros(max(nq, 1), dtype=np.uint32)
+        self._check(self._api.get_mapping(self._h, _p(ids, C.c_uint32), _p(pos, C.c_uint32), nq))
+        mapping = {int(i): int(p) for i, p in zip(ids[:nq], pos[:nq])}
+        return mapping, self.get_state(dtype=dtype)
+
+    # -- extensions (no reference counterpart) --------------------------------
+    def get_state(self, offset=0, count=None, dtype=np.complex128):
+        n = C.c_uint32()
+        self._check(self._api.num_qubits(self._h, C.byref(n)))
+        total = 1 << n.value
+        count = total - offset if count is None else count
+        dt = np.dtype(dtype)
+        code = _lib.GSIM_C64 if dt == np.complex64 else _lib.GSIM_C128
+        out = np.empty(count, dtype=np.complex64 if code == _lib.GSIM_C64 else np.complex128)
+        self._check(self._api.get_state(self._h, out.ctypes.data_as(C.c_void_p), code, offset, count))
+        return out
+
+    def set_fusion(self, mode="reference", kmax=0):
+        self._check(self._api.set_fusion(self._h, _FUSION[mode], int(kmax)))
+
+    def synchronize(self):
+        self._check(self._api.synchronize(self._h))
+
+    def reserve(self, nqubits):
+        self._check(self._api.reserve(self._h, int(nqubits)))
+
+    def counters(self):
+        out = np.zeros(4, dtype=np.uint64)
+        self._check(self._api.get_counters(self._h, _p(out, C.c_uint64), 4))
+        return {"logical_gates": int(out[0]), "gate_launches": int(out[1]), "gate_bytes": int(out[2]),
+                "gate_passes": int(out[3])}
+
+    def reset_counters(self):
+        self._check(self._api.reset_counters(self._h))
+
+    def device_state(self):
+        """(device pointer, number of amplitudes, "c64"|"c128") of the flushed state."""
+        ptr = C.c_void_p()
+        n = C.c_size_t()
+        dt = C.c_int()
+        self._check(self._api.state_device_ptr(self._h, C.byref(ptr), C.byref(n), C.byref(dt)))
+        return ptr.value, n.value, ("c64" if dt.value == _lib.GSIM_C64 else "c128")

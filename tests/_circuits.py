@@ -1,0 +1,67 @@
+"""Seeded random inputs for the parity tests (shared with the fixture
+generator tests/golden/make_golden.py)."""
+
+import numpy as np
+
+from projectq_gb300.workloads import H, Rx, Ry, Rz, S, T, X, Y, Z
+
+
+def haar_unitary(k, rng):
+    """Haar-random 2^k x 2^k unitary: QR of a complex Gaussian matrix with
+    the phases of diag(R) divided out."""
+    d = 1 << k
+    z = (rng.standard_normal((d, d)) + 1j * rng.standard_normal((d, d))) / np.sqrt(2.0)
+    q, r = np.linalg.qr(z)
+    ph = np.diag(r) / np.abs(np.diag(r))
+    return q * ph[None, :]
+
+
+def random_mixed_circuit(n, ngates, seed, kmax=5, max_ctrl=3):
+    """Gates of every shape the engine sees: named 1-qubit gates, rotations,
+    dense Haar gates on up to kmax qubits, with 0..max_ctrl controls."""
+    rng = np.random.default_rng(seed)
+    named = [H, X, Y, Z, S, T]
+    gates = []
+    for _ in range(ngates):
+        kind = rng.integers(4)
+        if kind == 0:
+            m = named[int(rng.integers(len(named)))]
+            k = 1
+        elif kind == 1:
+            m = [Rx, Ry, Rz][int(rng.integers(3))](float(rng.uniform(0, 4 * np.pi)))
+            k = 1
+        else:
+            k = int(rng.integers(1, min(kmax, n) + 1))
+            m = haar_unitary(k, rng)
+        nc = int(rng.integers(0, min(max_ctrl, n - k) + 1))
+        qs = [int(v) for v in rng.choice(n, size=k + nc, replace=False)]
+        gates.append((m, tuple(qs[:k]), tuple(qs[k:])))
+    return gates
+
+
+def random_pauli_sum(nq, nterms, seed, with_identity=True, p_identity=0.5):
+    rng = np.random.default_rng(seed)
+    terms = []
+    if with_identity:
+        terms.append(([], float(rng.standard_normal())))
+    for _ in range(nterms):
+        term = []
+        for q in range(nq):
+            if rng.uniform() < p_identity:
+                continue
+            term.append((q, "XYZ"[int(rng.integers(3))]))
+        terms.append((term, float(rng.standard_normal())))
+    return terms
+
+
+def run_circuit(sim, gates, run_each=False):
+    for m, t, c in gates:
+        sim.apply_controlled_gate(m, list(t), list(c))
+        if run_each:
+            sim.run()
+    sim.run()
+
+
+def allocate(sim, n):
+    for q in range(n):
+        sim.allocate_qubit(q)
