@@ -1,0 +1,379 @@
+#!/usr/bin/env python3
+"""Benchmark: 30-qubit random circuit on one GB300 — gates/s and HBM GB/s of
+the complex64 engine (FP64 reductions) next to the complex128 plain path.
+
+Workload (one "step"): the depth-40 random circuit of 30 qubits with 40 gates
+per layer over {H, T, S, Rx, Ry, Rz, CNOT, CZ, Toffoli} (seeded, numpy PCG64
+seed 0) applied to the device-resident state (8 GiB complex64; the complex128
+arm holds 16 GiB).  The initial state is i.i.d. complex Gaussian, normalised.
+Inputs are larger than L2 (129 MB), so no cache flush is needed between steps.
+
+Reported:
+  value     logical gates/s of the complex64 engine (device-resident state,
+            CUDA events on the engine's stream, max over ranks);
+  e2e       the same metric through the reference-facing Python API
+            (Simulator.set_wavefunction from pinned host memory, one
+            apply_controlled_gate call per gate, run, and a host read of
+            <Z0 Z1 + X5 X6> and a measurement) — host<->device copies inside;
+  c128      the complex128 plain path on the same circuit and GPU;
+  fidelity  1 - |<psi_c128|psi_c64>|^2 and max |d psi| after one circuit;
+  roofline  the dominant gate kernel's achieved algorithmic HBM GB/s
+            (bytes per launch / per-launch CUDA-event time) vs the measured
+            copy bandwidth in MEASURED_PEAKS.json;
+  cpu_baseline  the CPU oracle (a restatement of the reference engine, OpenMP
+            on all host cores) on a bounded sample of the same circuit.
+
+`--impl reference` times that CPU implementation alone on the same metric.
+Multi-GPU: the path runs as independent replicas (one per rank).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "30q circuit gates/s & HBM GB/s: c64+FP64-reduce vs c128 on GB300 at 1-F<=1e-6"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--per-layer", type=int, default=40)
+    ap.add_argument("--fusion", default="staged", choices=["staged", "reference", "none"])
+    ap.add_argument("--c128-steps", type=int, default=None, help="timed steps of the complex128 arm")
+    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--cpu-gates", type=int, default=24, help="gates in the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def __enter__(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except Exception:
+            self._proc = None
+        return self
+
+    def _read(self):
+        for line in self._proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self._proc is not None:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except Exception:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        return dist, world, rank, local
+    return None, 1, 0, 0
+
+
+def allreduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+def apply_circuit(sim, gates):
+    for m, t, c in gates:
+        sim.apply_controlled_gate(m, t, c)
+    sim.run()
+
+
+def timed_steps(sim, gates, steps, warmup, dist, profile_kernel=True):
+    for _ in range(warmup):
+        apply_circuit(sim, gates)
+    sim.synchronize()
+    sim.reset_counters()
+    barrier(dist)
+    sim.synchronize()
+    sim.profile(profile_kernel)
+    sim.timer_mark(0)
+    for _ in range(steps):
+        apply_circuit(sim, gates)
+    sim.timer_mark(1)
+    ms = sim.timer_elapsed(0, 1)
+    sim.synchronize()
+    barrier(dist)
+    recs = sim.profile_records() if profile_kernel else []
+    sim.profile(False)
+    return ms, sim.counters(), recs
+
+
+def dominant_kernel(recs):
+    """Group launches by kernel kind and width; the group with the most time."""
+    groups = {}
+    for r in recs:
+        key = (r["kind"], r["k"], r["precision"])
+        g = groups.setdefault(key, {"launches": 0, "ms": 0.0, "bytes": 0})
+        g["launches"] += 1
+        g["ms"] += r["ms"]
+        g["bytes"] += r["bytes"]
+    if not groups:
+        return None, {}
+    key = max(groups, key=lambda k: groups[k]["ms"])
+    return key, groups
+
+
+def cpu_baseline(gates, nq, ngates):
+    """The oracle port (OpenMP, all host threads) on the first `ngates` gates of
+    the circuit at full width, one pass per gate (the reference's run() per gate)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _backends import make
+
+    threads = os.cpu_count() or 1
+    sim = make("oracle", seed=0)
+    for q in range(nq):
+        sim.allocate_qubit(q)
+    sim.set_fusion("none")
+    sample = gates[:ngates]
+    t0 = time.perf_counter()
+    for m, t, c in sample:
+        sim.apply_controlled_gate(m, t, c)
+    sim.run()
+    dt = time.perf_counter() - t0
+    nbytes = sum(2 * (1 << (nq - len(c))) * 16 for _, _, c in sample)
+    del sim
+    return {"value": len(sample) / dt, "unit": "gates/s", "cores": threads, "kind": "port",
+            "sample": f"first {len(sample)} gates of the circuit at {nq} qubits, complex128, one pass per gate",
+            "hbm_like_gbs": nbytes / dt / 1e9, "seconds": dt}
+
+
+def host_memory_gib():
+    try:
+        return os.sysconf("SC_PAGE_SIZE") * os.sysconf("SC_PHYS_PAGES") / 2**30
+    except Exception:
+        return 0.0
+
+
+def run_reference(a):
+    """--impl reference: the CPU implementation on the machine's host cores."""
+    from projectq_gb300.workloads import config2_circuit
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
+    nq = a.qubits
+    need = 2 * (1 << nq) * 16 / 2**30 + 2
+    if host_memory_gib() and host_memory_gib() < need:
+        nq = max(20, int(math.log2(host_memory_gib() * 2**30 / 40)))
+    samples = []
+    for _ in range(a.warmup):
+        cpu_baseline(gates, nq, max(4, a.cpu_gates // 4))
+    for _ in range(a.steps):
+        samples.append(cpu_baseline(gates, nq, a.cpu_gates))
+    v = statistics.median(s["value"] for s in samples)
+    cb = dict(samples[0])
+    cb["value"] = v
+    print(json.dumps({
+        "metric": METRIC, "impl": "reference", "value": v, "unit": "gates/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * a.cpu_gates / v,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+        "data": "synthetic", "config": {"workload": f"random circuit, {nq} qubits, depth {a.depth}, "
+                                                    f"{a.per_layer} gates/layer (sample of {a.cpu_gates} gates)",
+                                        "qubits": nq},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": v, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+        return
+    dist, world, rank, local = dist_init()
+    from projectq_gb300 import Simulator
+    from projectq_gb300.simulator import pin_host, set_device
+    from projectq_gb300.workloads import config2_circuit, random_state
+
+    set_device(local)
+    nq = a.qubits
+    gates = config2_circuit(nq, a.depth, a.per_layer, seed=0)
+    G = len(gates)
+    psi0 = random_state(nq, seed=0, dtype=np.complex64)
+    ids = list(range(nq))
+
+    # --- accuracy: one circuit from psi0 on both precisions ------------------
+    s64 = Simulator(1, precision="c64", fusion=a.fusion)
+    for q in ids:
+        s64.allocate_qubit(q)
+    s64.set_wavefunction(psi0, ids)
+    s128 = Simulator(1, precision="c128", fusion=a.fusion)
+    for q in ids:
+        s128.allocate_qubit(q)
+    s128.set_wavefunction(psi0.astype(np.complex128), ids)
+    apply_circuit(s64, gates)
+    apply_circuit(s128, gates)
+    ip, maxerr = s128.compare(s64)
+    n128 = s128.compare(s128)[0].real
+    n64 = s64.compare(s64)[0].real
+    one_minus_f = 1.0 - abs(ip) ** 2 / (n128 * n64)
+
+    # --- timed: complex64 ------------------------------------------------------
+    with ClockSampler(local) as clk:
+        ms64, cnt64, recs = timed_steps(s64, gates, a.steps, a.warmup, dist)
+    ms64 = allreduce_max(dist, ms64)
+    key, groups = dominant_kernel(recs)
+    # --- timed: complex128 -----------------------------------------------------
+    k128 = a.c128_steps if a.c128_steps is not None else max(1, a.steps)
+    ms128, cnt128, _ = timed_steps(s128, gates, k128, max(1, min(a.warmup, 3)), dist, profile_kernel=False)
+    ms128 = allreduce_max(dist, ms128)
+    del s128
+
+    # --- e2e through the Python API, host buffers ------------------------------
+    pin = pin_host(psi0)
+    e2e_times = []
+    zz = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
+    e2e_sim = s64
+    for i in range(a.e2e_steps + 1):
+        e2e_sim.synchronize()
+        t0 = time.perf_counter()
+        e2e_sim.set_wavefunction(psi0, ids)
+        apply_circuit(e2e_sim, gates)
+        ev = e2e_sim.get_expectation_value(zz, ids)
+        bits = e2e_sim.measure_qubits(ids)
+        dt = time.perf_counter() - t0
+        if i > 0:  # the first call pays one-time host page-locking costs
+            e2e_times.append(dt)
+    pin.close()
+    e2e = allreduce_max(dist, statistics.median(e2e_times))
+
+    # --- CPU baseline (rank 0, N = 1 only) -------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cq = nq
+        if host_memory_gib() and host_memory_gib() < 2 * (1 << nq) * 16 / 2**30 + 8:
+            cq = 26
+        try:
+            cpu = cpu_baseline(gates, cq, a.cpu_gates)
+        except Exception as exc:  # pragma: no cover - host memory
+            cpu = {"value": None, "unit": "gates/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"failed: {exc}"}
+
+    if rank != 0:
+        return
+    peak, peak_src = measured_peak()
+    g = groups.get(key) if key else None
+    roofline = None
+    if g:
+        avg_bytes = g["bytes"] / g["launches"]
+        avg_ms = g["ms"] / g["launches"]
+        achieved = avg_bytes / (avg_ms * 1e-3) / 1e9
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
+                    "kernel": {"kind": ["dense_gate", "staged_tile"][key[0]], "k": key[1],
+                               "precision": "c64" if key[2] == 1 else "c128",
+                               "launches": g["launches"], "share": g["ms"] / max(1e-9, sum(x["ms"] for x in groups.values()))},
+                    "note": "achieved = algorithmic bytes per launch / mean per-launch CUDA-event time"}
+    value = world * G * a.steps / (ms64 * 1e-3)
+    v128 = world * G * k128 / (ms128 * 1e-3)
+    out = {
+        "metric": METRIC, "value": value, "unit": "gates/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms64 / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c64", "data": "synthetic",
+        "config": {"workload": f"random circuit, {nq} qubits, depth {a.depth}, {a.per_layer} gates/layer "
+                               f"({G} gates), complex64 state (FP64 reductions) vs complex128",
+                   "qubits": nq, "gates_per_step": G, "fusion": a.fusion,
+                   "l2": "inputs larger than L2 (state 8 GiB c64 / 16 GiB c128); no flush",
+                   "parallelism": f"replicas x{world}"},
+        "hbm_gbs": cnt64["gate_bytes"] / (ms64 * 1e-3) / 1e9,
+        "c128": {"value": v128, "unit": "gates/s", "ms_per_step": ms128 / k128, "steps": k128,
+                 "hbm_gbs": cnt128["gate_bytes"] / (ms128 * 1e-3) / 1e9},
+        "c64_over_c128": value / v128,
+        "accuracy": {"one_minus_fidelity": one_minus_f, "max_abs_err": maxerr, "reference": "engine c128 path"},
+        "e2e": {"value": world * G / e2e, "unit": "gates/s", "h2d_bytes_per_step": int(psi0.nbytes),
+                "d2h_bytes_per_step": 8 + nq, "seconds_per_step": e2e,
+                "path": "Simulator.set_wavefunction (pinned host c64) + apply_controlled_gate per gate + run "
+                        "+ get_expectation_value + measure_qubits"},
+        "gpu_launches": cnt64["gate_launches"],
+        "passes_per_step": cnt64["gate_passes"] / a.steps,
+        "roofline": roofline,
+        "cpu_baseline": cpu and {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "clocks": clk.summary(),
+        "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()},
+        "expectation_z0z1_x5x6": ev, "measured": int(sum(b << i for i, b in enumerate(bits))),
+    }
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -201,6 +201,45 @@ GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
 GSIM_API int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n);
 GSIM_API int gsim_reset_counters(gsim_engine *e);
 
+/* ---- Timing, device and host-memory helpers (no reference counterpart) ---- */
+
+/* FP64 inner product <a|b> and max_i |a_i - b_i| of two engines' flushed
+ * states (same device, same qubits and ordering; precisions may differ):
+ * out[0] = Re, out[1] = Im, out[2] = max. */
+GSIM_API int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out);
+
+/* Make `device` current for the calling thread before gsim_create. */
+GSIM_API int gsim_set_device(int device);
+
+/* Record CUDA event `slot` (0..15) on the engine's stream; gsim_timer_elapsed
+ * waits for event b and returns the milliseconds between events a and b. */
+GSIM_API int gsim_timer_mark(gsim_engine *e, int slot);
+GSIM_API int gsim_timer_elapsed(gsim_engine *e, int a, int b, float *ms);
+
+/* Per-launch profile of gate kernels: when enabled, every gate-kernel launch
+ * is bracketed by CUDA events on the engine's stream.  fetch waits for the
+ * stream and copies up to cap records. */
+typedef struct gsim_launch_record {
+  uint32_t kind;      /* 0 dense gate kernel, 1 staged tile kernel */
+  uint32_t k;         /* matrix qubits */
+  uint32_t nctrl;     /* control qubits */
+  uint32_t nqubits;   /* state qubits */
+  uint64_t targets;   /* bit mask of the matrix qubits' positions */
+  uint64_t bytes;     /* algorithmic bytes: 2 x touched amplitudes x bytes/amplitude */
+  uint32_t precision; /* GSIM_C128 or GSIM_C64 */
+  uint32_t ngates;    /* logical gates applied by the launch */
+  float ms;           /* device time of the launch */
+  float pad;
+} gsim_launch_record;
+GSIM_API int gsim_profile_enable(gsim_engine *e, int on);
+GSIM_API int gsim_profile_fetch(gsim_engine *e, gsim_launch_record *out, size_t cap, size_t *n);
+GSIM_API int gsim_profile_clear(gsim_engine *e);
+
+/* Page-lock (pin) a caller's host buffer so that set_wavefunction/get_state
+ * copies run at full link speed; unregister before freeing it. */
+GSIM_API int gsim_host_register(void *ptr, size_t bytes);
+GSIM_API int gsim_host_unregister(void *ptr);
+
 #ifdef __cplusplus
 }
 #endif

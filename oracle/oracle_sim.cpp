@@ -313,30 +313,60 @@ struct OSim {
   // Dense controlled k-qubit gate, the semantics of nointrin/kernel{1..5}.hpp:
   // for every index I with all target bits 0 and (I & ctrlmask) == ctrlmask,
   // v = psi[I + subsets of targets]; psi[...] <- M v.  Matrix bit l <-> pos[l].
-  void kernel(const std::vector<cplx> &M, const std::vector<unsigned> &pos, size_t ctrlmask) {
-    size_t k = pos.size(), d = size_t(1) << k;
+  // Loop structure as the reference's: an OpenMP loop over runs of indices
+  // below the lowest target bit (contiguous in memory), unrolled in k.
+  template <int K>
+  void kernel_k(const std::vector<cplx> &M, const std::vector<unsigned> &pos, size_t ctrlmask) {
+    constexpr size_t D = size_t(1) << K;
     std::vector<unsigned> sorted(pos.begin(), pos.end());
     std::sort(sorted.begin(), sorted.end());
-    std::vector<size_t> off(d, 0);
-    for (size_t j = 0; j < d; ++j)
-      for (size_t l = 0; l < k; ++l)
+    size_t off[D];
+    for (size_t j = 0; j < D; ++j) {
+      off[j] = 0;
+      for (size_t l = 0; l < K; ++l)
         if ((j >> l) & 1) off[j] |= size_t(1) << pos[l];
-    long long groups = (long long)(vec.size() >> k);
-#pragma omp parallel
-    {
-      std::vector<cplx> v(d);
-#pragma omp for schedule(static)
-      for (long long g = 0; g < groups; ++g) {
-        size_t I = size_t(g);
-        for (unsigned p : sorted) I = ((I >> p) << (p + 1)) | (I & ((size_t(1) << p) - 1));
+    }
+    double mr[D * D], mi[D * D];
+    for (size_t i = 0; i < D * D; ++i) {
+      mr[i] = M[i].real();
+      mi[i] = M[i].imag();
+    }
+    const unsigned p0 = sorted[0];
+    const size_t inner = size_t(1) << p0;
+    const long long runs = (long long)(vec.size() >> (K + p0));
+    double *psi = reinterpret_cast<double *>(vec.data());
+#pragma omp parallel for schedule(static)
+    for (long long r = 0; r < runs; ++r) {
+      size_t base = size_t(r) << p0;
+      for (unsigned p : sorted) base = ((base >> p) << (p + 1)) | (base & ((size_t(1) << p) - 1));
+      for (size_t x = 0; x < inner; ++x) {
+        const size_t I = base + x;
         if ((I & ctrlmask) != ctrlmask) continue;
-        for (size_t j = 0; j < d; ++j) v[j] = vec[I + off[j]];
-        for (size_t r = 0; r < d; ++r) {
-          cplx acc = 0.;
-          for (size_t j = 0; j < d; ++j) acc += M[r * d + j] * v[j];
-          vec[I + off[r]] = acc;
+        double vr[D], vi[D];
+        for (size_t j = 0; j < D; ++j) {
+          vr[j] = psi[2 * (I + off[j])];
+          vi[j] = psi[2 * (I + off[j]) + 1];
+        }
+        for (size_t a = 0; a < D; ++a) {
+          double sr = 0., si = 0.;
+          for (size_t j = 0; j < D; ++j) {
+            sr += mr[a * D + j] * vr[j] - mi[a * D + j] * vi[j];
+            si += mr[a * D + j] * vi[j] + mi[a * D + j] * vr[j];
+          }
+          psi[2 * (I + off[a])] = sr;
+          psi[2 * (I + off[a]) + 1] = si;
         }
       }
+    }
+  }
+  void kernel(const std::vector<cplx> &M, const std::vector<unsigned> &pos, size_t ctrlmask) {
+    switch (pos.size()) {
+      case 1: return kernel_k<1>(M, pos, ctrlmask);
+      case 2: return kernel_k<2>(M, pos, ctrlmask);
+      case 3: return kernel_k<3>(M, pos, ctrlmask);
+      case 4: return kernel_k<4>(M, pos, ctrlmask);
+      case 5: return kernel_k<5>(M, pos, ctrlmask);
+      default: fail(GSIM_ERR_VALUE, "Gates with more than 5 qubits are not supported!");
     }
   }
 

@@ -78,12 +78,38 @@ SIGNATURES = {
     "set_fusion": (C.c_int, [_eng, C.c_int, C.c_uint32]),
 }
 # Entry points only the product library has.
+class LaunchRecord(C.Structure):
+    """gsim_launch_record of include/gb300sim.h."""
+
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("k", C.c_uint32),
+        ("nctrl", C.c_uint32),
+        ("nqubits", C.c_uint32),
+        ("targets", C.c_uint64),
+        ("bytes", C.c_uint64),
+        ("precision", C.c_uint32),
+        ("ngates", C.c_uint32),
+        ("ms", C.c_float),
+        ("pad", C.c_float),
+    ]
+
+
 PRODUCT_ONLY = {
     "device_count": (C.c_int, []),
     "state_device_ptr": (C.c_int, [_eng, C.POINTER(C.c_void_p), C.POINTER(_sz), C.POINTER(C.c_int)]),
     "reserve": (C.c_int, [_eng, C.c_uint32]),
     "get_counters": (C.c_int, [_eng, _u64p, _sz]),
     "reset_counters": (C.c_int, [_eng]),
+    "set_device": (C.c_int, [C.c_int]),
+    "compare_states": (C.c_int, [_eng, _eng, _f64p]),
+    "timer_mark": (C.c_int, [_eng, C.c_int]),
+    "timer_elapsed": (C.c_int, [_eng, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "profile_enable": (C.c_int, [_eng, C.c_int]),
+    "profile_fetch": (C.c_int, [_eng, C.POINTER(LaunchRecord), _sz, C.POINTER(_sz)]),
+    "profile_clear": (C.c_int, [_eng]),
+    "host_register": (C.c_int, [C.c_void_p, _sz]),
+    "host_unregister": (C.c_int, [C.c_void_p]),
 }
 
 PKG = Path(__file__).resolve().parent

@@ -107,6 +107,9 @@ class Engine {
   }
   ~Engine() {
     if (stream_) cudaStreamSynchronize(stream_);
+    for (cudaEvent_t ev : timer_)
+      if (ev) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : ev_pool_) cudaEventDestroy(ev);
     for (DevBuf *b : {&state_, &scratch_, &part_, &small_, &aux1_, &aux2_, &aux3_, &table_, &table2_})
       b->release();
     pinned_.release();
@@ -517,6 +520,19 @@ class Engine {
   }
   void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
+  // <this|other>, max |this_i - other_i| (no reference counterpart).
+  void compare(Engine &other, double *out) {
+    run();
+    other.run();
+    if (N_ != other.N_ || map_ != other.map_)
+      fail(GSIM_ERR_VALUE, "compare_states(): the engines hold different qubits or orderings");
+    CK(cudaStreamSynchronize(other.stream_));
+    double *d_out = static_cast<double *>(small_.get(4096));
+    CK(launch_compare(prec_, state_.p, other.prec_, other.state_.p, uint64_t(1) << N_, part(), d_out, stream_));
+    CK(cudaMemcpyAsync(out, d_out, 24, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+  }
+
   void set_fusion(int mode, unsigned kmax) {
     run();
     if (mode != GSIM_FUSION_REFERENCE && mode != GSIM_FUSION_NONE && mode != GSIM_FUSION_STAGED)
@@ -525,6 +541,41 @@ class Engine {
     if (kmax) kmax_ = std::min(kmax, 5u);
   }
   void reserve(unsigned nq) { ensure_capacity(nq); }
+
+  // ---- timing -------------------------------------------------------------
+  void timer_mark(int slot) {
+    if (slot < 0 || slot >= 16) fail(GSIM_ERR_VALUE, "timer slot must be 0..15");
+    if (!timer_[slot]) CK(cudaEventCreate(&timer_[slot]));
+    CK(cudaEventRecord(timer_[slot], stream_));
+  }
+  float timer_elapsed(int a, int b) {
+    if (a < 0 || a >= 16 || b < 0 || b >= 16 || !timer_[a] || !timer_[b])
+      fail(GSIM_ERR_VALUE, "timer slots not recorded");
+    CK(cudaEventSynchronize(timer_[b]));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, timer_[a], timer_[b]));
+    return ms;
+  }
+  void profile_enable(bool on) {
+    run();
+    profiling_ = on;
+  }
+  size_t profile_fetch(gsim_launch_record *out, size_t cap) {
+    run();
+    CK(cudaStreamSynchronize(stream_));
+    size_t n = std::min(cap, prof_.size());
+    for (size_t i = 0; i < n; ++i) {
+      gsim_launch_record r = prof_[i].rec;
+      CK(cudaEventElapsedTime(&r.ms, ev_pool_[prof_[i].ev0], ev_pool_[prof_[i].ev1]));
+      out[i] = r;
+    }
+    return prof_.size();
+  }
+  void profile_clear() {
+    CK(cudaStreamSynchronize(stream_));
+    prof_.clear();
+    ev_next_ = 0;
+  }
   uint64_t counter(size_t i) const { return i < 4 ? counters_[i] : 0; }
   void reset_counters() { std::fill(std::begin(counters_), std::end(counters_), 0); }
 
@@ -594,12 +645,41 @@ class Engine {
     CK(cudaStreamSynchronize(stream_));
   }
 
-  void exec_dense(const DenseOp &op) {
-    CK(launch_dense(prec_, state_.p, N_, op, stream_));
+  void exec_dense(const DenseOp &op, uint32_t ngates = 1) {
     const unsigned c = unsigned(__builtin_popcountll(op.ctrl_mask));
+    const uint64_t bytes = 2 * (uint64_t(1) << (N_ - c)) * bpa_;
+    int e0 = -1;
+    if (profiling_) e0 = record_event();
+    CK(launch_dense(prec_, state_.p, N_, op, stream_));
+    if (profiling_) {
+      const int e1 = record_event();
+      Prof p;
+      std::memset(&p.rec, 0, sizeof(p.rec));
+      p.rec.kind = 0;
+      p.rec.k = uint32_t(op.pos.size());
+      p.rec.nctrl = c;
+      p.rec.nqubits = N_;
+      for (unsigned q : op.pos) p.rec.targets |= uint64_t(1) << q;
+      p.rec.bytes = bytes;
+      p.rec.precision = uint32_t(prec_);
+      p.rec.ngates = ngates;
+      p.ev0 = e0;
+      p.ev1 = e1;
+      prof_.push_back(p);
+    }
     counters_[1] += 1;
-    counters_[2] += 2 * (uint64_t(1) << (N_ - c)) * bpa_;
+    counters_[2] += bytes;
     counters_[3] += 1;
+  }
+  int record_event() {
+    if (ev_next_ >= ev_pool_.size()) {
+      cudaEvent_t ev;
+      CK(cudaEventCreate(&ev));
+      ev_pool_.push_back(ev);
+    }
+    const int i = int(ev_next_++);
+    CK(cudaEventRecord(ev_pool_[i], stream_));
+    return i;
   }
 
   void run_staged();
@@ -690,6 +770,16 @@ class Engine {
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
   uint64_t counters_[4] = {0, 0, 0, 0};
+  // timing
+  cudaEvent_t timer_[16] = {};
+  struct Prof {
+    gsim_launch_record rec;
+    int ev0, ev1;
+  };
+  bool profiling_ = false;
+  std::vector<Prof> prof_;
+  std::vector<cudaEvent_t> ev_pool_;
+  size_t ev_next_ = 0;
 };
 
 // Sequential reference loop over [b0, b0 + cnt) starting from running sum P.
@@ -812,8 +902,9 @@ void Engine::run_staged() {
     gates.push_back(std::move(sg));
   }
   StagePlanner planner(N_, prec_, kmax_);
-  std::vector<DenseOp> ops = planner.fuse(gates);
-  for (auto const &op : ops) exec_dense(op);
+  std::vector<uint32_t> counts;
+  std::vector<DenseOp> ops = planner.fuse(gates, &counts);
+  for (size_t i = 0; i < ops.size(); ++i) exec_dense(ops[i], counts[i]);
 }
 
 }  // namespace gsim
@@ -823,6 +914,7 @@ void Engine::run_staged() {
 // ===========================================================================
 using gsim::Engine;
 using gsim::Error;
+using gsim::fail;
 
 namespace {
 template <class F>
@@ -1113,6 +1205,33 @@ int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n) {
 }
 int gsim_reset_counters(gsim_engine *e) {
   return guard([&] { E(e)->reset_counters(); });
+}
+int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out) {
+  return guard([&] { E(a)->compare(*E(b), out); });
+}
+int gsim_set_device(int device) {
+  return guard([&] { CK(cudaSetDevice(device)); });
+}
+int gsim_timer_mark(gsim_engine *e, int slot) {
+  return guard([&] { E(e)->timer_mark(slot); });
+}
+int gsim_timer_elapsed(gsim_engine *e, int a, int b, float *ms) {
+  return guard([&] { *ms = E(e)->timer_elapsed(a, b); });
+}
+int gsim_profile_enable(gsim_engine *e, int on) {
+  return guard([&] { E(e)->profile_enable(on != 0); });
+}
+int gsim_profile_fetch(gsim_engine *e, gsim_launch_record *out, size_t cap, size_t *n) {
+  return guard([&] { *n = E(e)->profile_fetch(out, cap); });
+}
+int gsim_profile_clear(gsim_engine *e) {
+  return guard([&] { E(e)->profile_clear(); });
+}
+int gsim_host_register(void *ptr, size_t bytes) {
+  return guard([&] { CK(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault)); });
+}
+int gsim_host_unregister(void *ptr) {
+  return guard([&] { CK(cudaHostUnregister(ptr)); });
 }
 
 }  // extern "C"

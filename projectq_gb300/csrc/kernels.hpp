@@ -111,4 +111,9 @@ cudaError_t launch_math_scatter(int prec, const void *in, void *out, unsigned nq
                                 const MathRegsDev &regs, const uint32_t *d_table,
                                 cudaStream_t s);
 
+// <a|b> and max_i |a_i - b_i| of two state vectors (FP64): d_out[0] = Re,
+// d_out[1] = Im, d_out[2] = max.  d_part: >= 4096 doubles.
+cudaError_t launch_compare(int prec_a, const void *a, int prec_b, const void *b, uint64_t n,
+                           double *d_part, double *d_out, cudaStream_t s);
+
 }  // namespace gsim

@@ -475,7 +475,46 @@ __global__ void __launch_bounds__(256) math_gather_kernel(const cplx_t<T> *__res
   }
 }
 
+template <typename A, typename B>
+__global__ void __launch_bounds__(256) compare_kernel(const A *__restrict__ a, const B *__restrict__ b,
+                                                      uint64_t n, double *part, int nblk,
+                                                      unsigned long long *maxbits) {
+  double re = 0., im = 0., mx = 0.;
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const double ar = a[i].x, ai = a[i].y, br = b[i].x, bi = b[i].y;
+    re = fma(ar, br, fma(ai, bi, re));   // Re(conj(a) b)
+    im = fma(ar, bi, fma(-ai, br, im));  // Im(conj(a) b)
+    const double dr = ar - br, di = ai - bi;
+    mx = fmax(mx, sqrt(fma(dr, dr, di * di)));
+  }
+  re = block_sum(re);
+  if (threadIdx.x == 0) part[blockIdx.x] = re;
+  im = block_sum(im);
+  if (threadIdx.x == 0) part[nblk + blockIdx.x] = im;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_down_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(maxbits, static_cast<unsigned long long>(__double_as_longlong(mx)));
+}
+
 }  // namespace
+
+cudaError_t launch_compare(int pa, const void *a, int pb, const void *b, uint64_t n, double *d_part,
+                           double *d_out, cudaStream_t s) {
+  const int nblk = int(std::min<unsigned>(grid(n, 256), 2048));
+  cudaMemsetAsync(d_out + 2, 0, 8, s);
+  auto *mx = reinterpret_cast<unsigned long long *>(d_out + 2);
+  if (pa == 1 && pb == 1)
+    compare_kernel<float2, float2><<<nblk, 256, 0, s>>>(static_cast<const float2 *>(a), static_cast<const float2 *>(b), n, d_part, nblk, mx);
+  else if (pa == 1 && pb == 0)
+    compare_kernel<float2, double2><<<nblk, 256, 0, s>>>(static_cast<const float2 *>(a), static_cast<const double2 *>(b), n, d_part, nblk, mx);
+  else if (pa == 0 && pb == 1)
+    compare_kernel<double2, float2><<<nblk, 256, 0, s>>>(static_cast<const double2 *>(a), static_cast<const float2 *>(b), n, d_part, nblk, mx);
+  else
+    compare_kernel<double2, double2><<<nblk, 256, 0, s>>>(static_cast<const double2 *>(a), static_cast<const double2 *>(b), n, d_part, nblk, mx);
+  column_sums_kernel<<<2, 256, 0, s>>>(d_part, nblk, d_out);
+  return cudaGetLastError();
+}
 
 // ---- launchers -------------------------------------------------------------
 

@@ -31,7 +31,8 @@ class StagePlanner {
   StagePlanner(unsigned nq, int prec, unsigned kmax)
       : nq_(nq), kmax_(std::max(1u, std::min(kmax, prec == 1 ? 4u : 2u))) {}
 
-  std::vector<DenseOp> fuse(const std::vector<StageGate> &gates) const {
+  std::vector<DenseOp> fuse(const std::vector<StageGate> &gates,
+                            std::vector<uint32_t> *counts = nullptr) const {
     std::vector<DenseOp> out;
     size_t i = 0;
     while (i < gates.size()) {
@@ -49,6 +50,7 @@ class StagePlanner {
         ++j;
       }
       out.push_back(compose(gates, i, j, qubits, shared));
+      if (counts) counts->push_back(uint32_t(j - i));
       i = j;
     }
     return out;

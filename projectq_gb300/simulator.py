@@ -353,3 +353,56 @@ class Simulator:
         dt = C.c_int()
         self._check(self._api.state_device_ptr(self._h, C.byref(ptr), C.byref(n), C.byref(dt)))
         return ptr.value, n.value, ("c64" if dt.value == _lib.GSIM_C64 else "c128")
+
+    def compare(self, other):
+        """(<self|other> as complex, max |self_i - other_i|), FP64 on the device."""
+        out = np.zeros(3, dtype=np.float64)
+        self._check(self._api.compare_states(self._h, other._h, _p(out, C.c_double)))
+        return complex(out[0], out[1]), float(out[2])
+
+    def timer_mark(self, slot):
+        """Record CUDA event `slot` (0..15) on the engine's stream."""
+        self._check(self._api.timer_mark(self._h, int(slot)))
+
+    def timer_elapsed(self, a, b):
+        """Milliseconds between events a and b (waits for b)."""
+        ms = C.c_float()
+        self._check(self._api.timer_elapsed(self._h, int(a), int(b), C.byref(ms)))
+        return ms.value
+
+    def profile(self, on=True):
+        """Bracket every gate-kernel launch with CUDA events (see profile_records)."""
+        self._check(self._api.profile_enable(self._h, 1 if on else 0))
+
+    def profile_records(self, clear=True):
+        """Per-launch records: dicts of kind, k, nctrl, nqubits, targets, bytes, ms, ngates."""
+        n = C.c_size_t()
+        self._check(self._api.profile_fetch(self._h, None, 0, C.byref(n)))
+        buf = (_lib.LaunchRecord * max(1, n.value))()
+        self._check(self._api.profile_fetch(self._h, buf, n.value, C.byref(n)))
+        out = [{f: getattr(r, f) for f, _ in _lib.LaunchRecord._fields_ if f != "pad"} for r in buf[: n.value]]
+        if clear:
+            self._check(self._api.profile_clear(self._h))
+        return out
+
+
+def pin_host(array: np.ndarray):
+    """Page-lock a NumPy array's memory (returns an object whose close()
+    unpins it) so host<->device copies through the engine run at link speed."""
+    api = _lib.load()
+    ptr = array.ctypes.data_as(C.c_void_p)
+    _lib.check(api, api.host_register(ptr, array.nbytes))
+
+    class _Pin:
+        def close(self_inner):
+            if getattr(self_inner, "_done", False):
+                return
+            _lib.check(api, api.host_unregister(ptr))
+            self_inner._done = True
+
+    return _Pin()
+
+
+def set_device(device: int):
+    api = _lib.load()
+    _lib.check(api, api.set_device(int(device)))

@@ -1,6 +1,8 @@
 """Seeded random inputs for the parity tests (shared with the fixture
 generator tests/golden/make_golden.py)."""
 
+from fractions import Fraction
+
 import numpy as np
 
 from projectq_gb300.workloads import H, Rx, Ry, Rz, S, T, X, Y, Z
@@ -65,3 +67,14 @@ def run_circuit(sim, gates, run_each=False):
 def allocate(sim, n):
     for q in range(n):
         sim.allocate_qubit(q)
+
+
+def fma(a, b, c):
+    """a*b + c with a single rounding (exact rational arithmetic, then the
+    correctly rounded float): the value of C's fma()."""
+    return float(Fraction(a) * Fraction(b) + Fraction(c))
+
+
+def norm2(z):
+    """|z|^2 as the reference's std::norm compiles with FMA: fma(re, re, im*im)."""
+    return fma(z.real, z.real, z.imag * z.imag)

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 from _backends import make
-from _circuits import allocate, haar_unitary, random_mixed_circuit, random_pauli_sum, run_circuit
+from _circuits import allocate, haar_unitary, norm2, random_mixed_circuit, random_pauli_sum, run_circuit
 from projectq_gb300.workloads import H, X, Z, mt19937_uniform, random_state
 
 pytestmark = pytest.mark.gpu
@@ -99,7 +99,7 @@ def _sequential_pick(psi, rnd):
     for z in psi:
         if not P < rnd:
             break
-        P += math.fma(z.real, z.real, z.imag * z.imag)
+        P += norm2(z)
         pick += 1
     return pick - 1
 
@@ -110,7 +110,7 @@ def test_measure_at_draws_bit_exact(n):
     sequential FP64 sampling rule, including draws placed exactly on running
     sums (n = 18 exercises the blocked replay, n = 9 the host loop)."""
     psi = random_state(n, seed=21)
-    norms = np.array([math.fma(z.real, z.real, z.imag * z.imag) for z in psi[: 1 << min(n, 12)]])
+    norms = [norm2(z) for z in psi[: 1 << min(n, 12)]]
     running = []
     P = 0.0
     for x in norms:
