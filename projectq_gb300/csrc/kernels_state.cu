@@ -637,7 +637,10 @@ cudaError_t launch_pauli_expect(int prec, const void *psi, unsigned nq, uint64_t
       const PauliTermDev &pt = h_terms[t0 + t];
       B.t[t].sign_mask = pt.sign_mask;
       if (hbit < 0) {
-        B.t[t].factor = 1.f;
+        // Diagonal term: Re[(-i)^q] |psi_i|^2 (q odd only for products of
+        // factors on one qubit, e.g. Y X = -i Z, whose real part is 0).
+        const int q = pt.phase & 3;
+        B.t[t].factor = q == 0 ? 1.f : q == 2 ? -1.f : 0.f;
         B.t[t].which = 0;
       } else {
         // c = (-1)^popcount(x & sign_mask); q = #Y mod 4 (see header).

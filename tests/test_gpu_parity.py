@@ -6,8 +6,6 @@ and complex64 to 5e-6; measurement outcomes at a given uniform draw and
 emulate_math permutations are compared exactly.
 """
 
-import math
-
 import numpy as np
 import pytest
 
