@@ -62,6 +62,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=1)
     ap.add_argument("--cpu-gates", type=int, default=24, help="gates in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--only", choices=["c64", "c128"], default=None,
+                    help="profiling mode: time one precision only (no accuracy, e2e or CPU legs)")
+    ap.add_argument("--init", choices=["random", "zero"], default="random",
+                    help="initial state; kernel times do not depend on the amplitudes")
     return ap.parse_args()
 
 
@@ -255,10 +259,31 @@ def run_reference(a):
     }), flush=True)
 
 
+def run_only(a):
+    """Profiling mode: the circuit on one precision, from |0...0> or psi0."""
+    from projectq_gb300 import Simulator
+    from projectq_gb300.workloads import config2_circuit, random_state
+
+    gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
+    sim = Simulator(1, precision=a.only, fusion=a.fusion)
+    for q in range(a.qubits):
+        sim.allocate_qubit(q)
+    if a.init == "random":
+        sim.set_wavefunction(random_state(a.qubits, seed=0, dtype=np.complex64), list(range(a.qubits)))
+    ms, cnt, recs = timed_steps(sim, gates, a.steps, a.warmup, None)
+    key, groups = dominant_kernel(recs)
+    print(json.dumps({"mode": "only", "precision": a.only, "qubits": a.qubits, "ms_per_step": ms / max(1, a.steps),
+                      "gates_per_s": len(gates) * a.steps / (ms * 1e-3), "counters": cnt,
+                      "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+        return
+    if a.only:
+        run_only(a)
         return
     dist, world, rank, local = dist_init()
     from projectq_gb300 import Simulator
