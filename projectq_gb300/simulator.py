@@ -18,6 +18,7 @@ libgb300sim.so; there is no CPU fallback.
 
 from __future__ import annotations
 
+import atexit
 import ctypes as C
 import numbers
 
@@ -29,6 +30,21 @@ _PRECISIONS = {"c128": _lib.GSIM_C128, "complex128": _lib.GSIM_C128, "c64": _lib
                "complex64": _lib.GSIM_C64}
 _FUSION = {"reference": _lib.GSIM_FUSION_REFERENCE, "none": _lib.GSIM_FUSION_NONE,
            "staged": _lib.GSIM_FUSION_STAGED}
+
+
+_PENDING = []
+
+
+def _release_pending():
+    while _PENDING:
+        api, h = _PENDING.pop()
+        try:
+            api.destroy(h)
+        except Exception:  # pragma: no cover - interpreter shutdown
+            pass
+
+
+atexit.register(_release_pending)
 
 
 def _u32(seq) -> np.ndarray:
@@ -99,6 +115,7 @@ class Simulator:
             raise TypeError("Simulator(): seed must be an unsigned 32-bit integer")
         if rnd_seed < 0 or rnd_seed > 0xFFFFFFFF:
             raise TypeError("Simulator(): seed must be an unsigned 32-bit integer")
+        _release_pending()
         self._api = _api if _api is not None else _lib.load()
         self._prec = _PRECISIONS[precision]
         h = C.c_void_p()
@@ -111,14 +128,29 @@ class Simulator:
     def _check(self, rc):
         _lib.check(self._api, rc)
 
-    def __del__(self):
-        h = getattr(self, "_h", None)
+    def close(self):
+        """Free the engine's device memory now (the object is unusable after)."""
+        h = self.__dict__.get("_h")
         if h is not None and h.value:
-            try:
-                self._api.destroy(h)
-            except Exception:  # pragma: no cover - interpreter shutdown
-                pass
-            self._h = None
+            self._api.destroy(h)
+        self.__dict__["_h"] = None
+
+    def __del__(self):
+        # Deferred: in a reference cycle (ProjectQ's MainEngine <-> backend)
+        # Python may finalize this object before MainEngine.__del__ flushes
+        # through it, as pybind11 objects are only freed after all finalizers.
+        # The handle is destroyed at the next construction, close() or exit.
+        h = self.__dict__.get("_h")
+        if h is not None and h.value:
+            _PENDING.append((self._api, h))
+
+    def __getattribute__(self, name):
+        if name == "_h":
+            h = object.__getattribute__(self, "__dict__").get("_h")
+            if h is None:
+                raise RuntimeError("the simulator engine has been closed")
+            return h
+        return object.__getattribute__(self, name)
 
     @property
     def precision(self) -> str:
