@@ -240,6 +240,25 @@ GSIM_API int gsim_profile_clear(gsim_engine *e);
 GSIM_API int gsim_host_register(void *ptr, size_t bytes);
 GSIM_API int gsim_host_unregister(void *ptr);
 
+/* ---- Allocation-free probability (no counterpart in the reference) ----------
+ * Sum of |psi_i|^2 over the indices i with (i & mask) == value, for a state
+ * vector the caller owns in device memory (2^nqubits amplitudes of
+ * `precision`), written to the host double *out after waiting on `stream`
+ * (a cudaStream_t; NULL = the legacy default stream).  For callers that
+ * cannot allocate device memory at the point of the call — code whose device
+ * memory belongs to another allocator (a framework's caching pool that must
+ * see every allocation), or a thread that must not take the CUDA allocator's
+ * locks while other work owns the device: it calls no cudaMalloc/cudaFree or
+ * allocating library routine; its partial sums live in a fixed ~32 KB
+ * __device__ array that every GPU loading the library keeps until exit.
+ * Limit: the summed subspace (2^(nqubits - popcount(mask)) amplitudes) may
+ * hold at most 2^32 amplitudes; larger requests fail with GSIM_ERR_LENGTH.
+ * The first call on a device resolves the array's address (make it before
+ * any stream capture); calls that overlap on the GPU share the array and
+ * race, so serialise them. */
+GSIM_API int gsim_probability_noalloc(const void *d_state, int precision, uint32_t nqubits,
+                                      uint64_t mask, uint64_t value, double *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -110,6 +110,10 @@ PRODUCT_ONLY = {
     "profile_clear": (C.c_int, [_eng]),
     "host_register": (C.c_int, [C.c_void_p, _sz]),
     "host_unregister": (C.c_int, [C.c_void_p]),
+    "probability_noalloc": (
+        C.c_int,
+        [C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, _f64p, C.c_void_p],
+    ),
 }
 
 PKG = Path(__file__).resolve().parent
