@@ -110,9 +110,11 @@ class Engine {
     for (cudaEvent_t ev : timer_)
       if (ev) cudaEventDestroy(ev);
     for (cudaEvent_t ev : ev_pool_) cudaEventDestroy(ev);
-    for (DevBuf *b : {&state_, &scratch_, &part_, &small_, &aux1_, &aux2_, &aux3_, &table_, &table2_})
+    for (DevBuf *b : {&state_, &scratch_, &part_, &small_, &aux1_, &aux2_, &aux3_, &table_, &table2_, &upload_dev_})
       b->release();
     pinned_.release();
+    upload_host_.release();
+    if (upload_ev_) cudaEventDestroy(upload_ev_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -539,6 +541,10 @@ class Engine {
       fail(GSIM_ERR_VALUE, "unknown fusion mode");
     mode_ = mode;
     if (kmax) kmax_ = std::min(kmax, 5u);
+    if (mode == GSIM_FUSION_STAGED && kmax >= 6) {  // kmax >= 6 selects the tile width in staged mode
+      tile_bits_c64_ = std::min(kmax, 14u);
+      tile_bits_c128_ = std::min(kmax - 1, 13u);
+    }
   }
   void reserve(unsigned nq) { ensure_capacity(nq); }
 
@@ -683,6 +689,7 @@ class Engine {
   }
 
   void run_staged();
+  void exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool);
 
   double masked_norm_host(uint64_t mask, uint64_t val) {
     double *d_norm = static_cast<double *>(small_.get(4096));
@@ -769,6 +776,10 @@ class Engine {
   unsigned fmin_ = 4, fmax_ = 5, max_gate_ = 5, kmax_ = 5;
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
+  unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
+  DevBuf upload_dev_;
+  HostBuf upload_host_;
+  cudaEvent_t upload_ev_ = nullptr;
   uint64_t counters_[4] = {0, 0, 0, 0};
   // timing
   cudaEvent_t timer_[16] = {};
@@ -891,7 +902,6 @@ void Engine::run_staged() {
   if (queue_.empty()) return;
   std::vector<QueuedGate> q;
   q.swap(queue_);
-  // Plan stages over the queue; each stage is one pass over the state.
   std::vector<StageGate> gates;
   gates.reserve(q.size());
   for (auto &g : q) {
@@ -901,10 +911,78 @@ void Engine::run_staged() {
     for (unsigned c : g.ctrl) sg.ctrl_mask |= uint64_t(1) << pos_of(c);
     gates.push_back(std::move(sg));
   }
-  StagePlanner planner(N_, prec_, kmax_);
-  std::vector<uint32_t> counts;
-  std::vector<DenseOp> ops = planner.fuse(gates, &counts);
-  for (size_t i = 0; i < ops.size(); ++i) exec_dense(ops[i], counts[i]);
+  // Tiles of 32 KB: 2^12 complex64 or 2^11 complex128 amplitudes, with runs
+  // of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
+  const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
+  const unsigned m = prec_ == GSIM_C64 ? 5 : 4;
+  StagePlanner planner(N_, L, m);
+  std::vector<PlanStep> steps = planner.plan(gates);
+  // Serialise every stage's operations and matrices into one upload.
+  const size_t esz = bpa_;
+  size_t bytes = 0;
+  std::vector<size_t> off_ops(steps.size()), off_pool(steps.size());
+  for (size_t i = 0; i < steps.size(); ++i) {
+    if (!steps[i].is_stage) continue;
+    off_ops[i] = bytes;
+    bytes += (steps[i].stage.ops.size() * sizeof(StageOpDev) + 15) / 16 * 16;
+    off_pool[i] = bytes;
+    bytes += (steps[i].stage.pool.size() * esz + 15) / 16 * 16;
+  }
+  char *dev = nullptr;
+  if (bytes) {
+    if (upload_ev_) CK(cudaEventSynchronize(upload_ev_));  // the staging buffer is free again
+    char *host = static_cast<char *>(upload_host_.get(bytes));
+    for (size_t i = 0; i < steps.size(); ++i) {
+      if (!steps[i].is_stage) continue;
+      const StagePlan &sp = steps[i].stage;
+      std::memcpy(host + off_ops[i], sp.ops.data(), sp.ops.size() * sizeof(StageOpDev));
+      if (prec_ == GSIM_C64) {
+        float *f = reinterpret_cast<float *>(host + off_pool[i]);
+        for (size_t j = 0; j < sp.pool.size(); ++j) {
+          f[2 * j] = float(sp.pool[j].real());
+          f[2 * j + 1] = float(sp.pool[j].imag());
+        }
+      } else {
+        std::memcpy(host + off_pool[i], sp.pool.data(), sp.pool.size() * 16);
+      }
+    }
+    dev = static_cast<char *>(upload_dev_.get(bytes));
+    CK(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, stream_));
+    if (!upload_ev_) CK(cudaEventCreateWithFlags(&upload_ev_, cudaEventDisableTiming));
+    CK(cudaEventRecord(upload_ev_, stream_));
+  }
+  for (size_t i = 0; i < steps.size(); ++i) {
+    if (!steps[i].is_stage) {
+      exec_dense(steps[i].dense);
+      continue;
+    }
+    exec_stage(steps[i].stage, dev + off_ops[i], dev + off_pool[i]);
+  }
+}
+
+void Engine::exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool) {
+  const uint64_t bytes = 2 * (uint64_t(1) << N_) * bpa_;
+  int e0 = -1;
+  if (profiling_) e0 = record_event();
+  CK(launch_stage(prec_, state_.p, N_, sp, d_ops, d_pool, stream_));
+  if (profiling_) {
+    const int e1 = record_event();
+    Prof p;
+    std::memset(&p.rec, 0, sizeof(p.rec));
+    p.rec.kind = 1;
+    p.rec.k = uint32_t(sp.ops.size());
+    p.rec.nqubits = N_;
+    for (unsigned q : sp.lpos) p.rec.targets |= uint64_t(1) << q;
+    p.rec.bytes = bytes;
+    p.rec.precision = uint32_t(prec_);
+    p.rec.ngates = sp.ngates;
+    p.ev0 = e0;
+    p.ev1 = e1;
+    prof_.push_back(p);
+  }
+  counters_[1] += 1;
+  counters_[2] += bytes;
+  counters_[3] += 1;
 }
 
 }  // namespace gsim

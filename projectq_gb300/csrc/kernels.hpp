@@ -8,25 +8,19 @@
 #include <cstdint>
 #include <vector>
 
+#include "ops.hpp"
+
 namespace gsim {
-
-using cplx = std::complex<double>;
-
-// One controlled dense k-qubit gate on bit positions pos[] (matrix bit l is
-// pos[l]); the gate acts where (index & ctrl_mask) == ctrl_mask.
-struct DenseOp {
-  std::vector<cplx> m;        // 2^k x 2^k, row-major, FP64
-  std::vector<unsigned> pos;  // k distinct bit positions
-  uint64_t ctrl_mask = 0;
-};
 
 // prec: 0 = complex128 state, 1 = complex64 state.
 cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s);
 
 // ---- stage kernel (many gates per pass through shared-memory tiles) -----
 struct StagePlan;  // defined in stage.hpp
-cudaError_t launch_stage(int prec, void *psi, unsigned nq, const StagePlan &plan,
-                         const void *d_ops, cudaStream_t s);
+// d_ops: the plan's StageOpDev array, d_pool: its matrices in the state's
+// precision, both already in device memory.
+cudaError_t launch_stage(int prec, void *psi, unsigned nq, const StagePlan &plan, const void *d_ops,
+                         const void *d_pool, cudaStream_t s);
 
 // ---- reductions and state kernels (kernels_state.cu) ---------------------
 // Sum over indices i with (i & mask) == val of |psi_i|^2 (FP64 accumulation).

@@ -1,22 +1,38 @@
-// Fusion planner used by GSIM_FUSION_STAGED: groups consecutive gates into
-// clusters of at most kmax matrix qubits and composes each cluster in FP64.
+// Stage planner for GSIM_FUSION_STAGED: many gates per pass over the state.
 //
-// Difference from the reference's greedy rule (fusion.hpp + simulator.hpp:
-// 204-222): clusters close only when the next gate would not fit (no eager
-// run at 4 qubits), the width limit follows the storage precision (complex64
-// gates stay HBM-bound up to 4 matrix qubits on GB300's FP32 pipes, while
-// complex128 is FP64-bound, so clusters there stay at 2 qubits, where fusing
-// costs no extra FP64 work per amplitude), and a control shared by all gates
-// of a cluster stays a control.  The composed unitary is the ordered product
-// of the same gates, so results agree with unfused application to rounding.
+// A stage is one pass of the stage kernel (kernels_stage.cu) over the state.
+// The state is cut into tiles of 2^L amplitudes that share the values of all
+// "non-local" bits; a tile's local bits are the m lowest bit positions (so
+// each tile is made of 2^(L-m) contiguous runs of 2^m amplitudes, read and
+// written with coalesced 16-byte accesses) plus up to L-m higher positions
+// chosen per stage.  A CTA loads a tile into shared memory, applies the
+// stage's operations in order, and writes it back.
+//
+//  - A non-diagonal gate needs its targets local; its controls can be
+//    anywhere (local: checked per amplitude, non-local: per tile).
+//  - A diagonal gate (Z, S, T, Rz, Ph, CZ, controlled phases...) needs no
+//    locality at all: it becomes a diagonal operation over its targets and
+//    controls, evaluated from the amplitude's global index.
+//  - Gates with more than 2 non-diagonal targets leave the stage and run as
+//    their own dense kernel.
+//
+// Planning is greedy in circuit order with a look-ahead window: a gate that
+// does not fit blocks its qubits, and later gates that touch no blocked
+// qubit (so they commute with every skipped gate) still join the stage.
+// Inside a stage, consecutive operations on the same targets and controls are
+// multiplied together, and runs of diagonal operations are merged (FP64).
+// The reference has no counterpart (its fusion is fusion.hpp's dense
+// clusters); the results equal applying the same gates one by one, up to
+// rounding.
 #pragma once
 
 #include <algorithm>
 #include <complex>
 #include <cstdint>
+#include <cstring>
 #include <vector>
 
-#include "kernels.hpp"
+#include "ops.hpp"
 
 namespace gsim {
 
@@ -26,98 +42,273 @@ struct StageGate {
   uint64_t ctrl_mask = 0;     // control bit positions
 };
 
+// Device-side description of one operation of a stage (see kernels_stage.cu).
+struct StageOpDev {
+  uint32_t kind;     // 0: dense on local targets, 1: diagonal
+  uint32_t k;        // number of targets (dense) or diagonal qubits
+  uint32_t mat;      // offset of the matrix / diagonal in the stage's pool (complex elements)
+  uint32_t lctrl;    // local controls (tile-bit mask)
+  uint64_t gctrl;    // non-local controls (global bit mask)
+  uint8_t tbit[8];   // tile-bit index of target / diagonal qubit j, 0xFF if non-local
+  uint8_t gbit[8];   // global bit position of diagonal qubit j
+};
+
+struct StagePlan {
+  unsigned L = 0;                 // tile bits
+  std::vector<unsigned> lpos;     // ascending global positions of the tile bits (lpos[i] = i for i < m)
+  std::vector<StageOpDev> ops;
+  std::vector<cplx> pool;         // matrices / diagonals, FP64 (converted at upload)
+  uint32_t ngates = 0;            // logical gates applied
+};
+
+// One step of the plan: either a stage or a single wide dense gate.
+struct PlanStep {
+  bool is_stage = true;
+  StagePlan stage;
+  DenseOp dense;
+  uint32_t ngates = 1;
+};
+
 class StagePlanner {
  public:
-  StagePlanner(unsigned nq, int prec, unsigned kmax)
-      : nq_(nq), kmax_(std::max(1u, std::min(kmax, prec == 1 ? 4u : 2u))) {}
+  // L: tile bits; m: contiguous low bits; window: look-ahead in gates.
+  StagePlanner(unsigned nq, unsigned L, unsigned m, size_t window = 512)
+      : nq_(nq), L_(std::min(L, nq)), m_(std::min(m, std::min(L, nq))), window_(window) {}
 
-  std::vector<DenseOp> fuse(const std::vector<StageGate> &gates,
-                            std::vector<uint32_t> *counts = nullptr) const {
-    std::vector<DenseOp> out;
-    size_t i = 0;
-    while (i < gates.size()) {
-      // Grow a cluster starting at gate i.
-      uint64_t shared = gates[i].ctrl_mask;
-      uint64_t qubits = mask_of(gates[i].pos);
-      size_t j = i + 1;
-      while (j < gates.size()) {
-        const StageGate &g = gates[j];
-        const uint64_t ns = shared & g.ctrl_mask;
-        const uint64_t nq = qubits | mask_of(g.pos) | (shared & ~ns) | (g.ctrl_mask & ~ns);
-        if (unsigned(__builtin_popcountll(nq)) > kmax_) break;
-        shared = ns;
-        qubits = nq;
-        ++j;
+  std::vector<PlanStep> plan(const std::vector<StageGate> &gates) const {
+    // Classify every gate once.
+    std::vector<Item> items(gates.size());
+    for (size_t i = 0; i < gates.size(); ++i) items[i] = classify(gates[i]);
+    std::vector<PlanStep> steps;
+    std::vector<char> done(gates.size(), 0);
+    size_t first = 0;
+    while (true) {
+      while (first < gates.size() && done[first]) ++first;
+      if (first >= gates.size()) break;
+      if (items[first].wide) {
+        PlanStep st;
+        st.is_stage = false;
+        st.dense.m = gates[first].m;
+        st.dense.pos = gates[first].pos;
+        st.dense.ctrl_mask = gates[first].ctrl_mask;
+        steps.push_back(std::move(st));
+        done[first] = 1;
+        continue;
       }
-      out.push_back(compose(gates, i, j, qubits, shared));
-      if (counts) counts->push_back(uint32_t(j - i));
-      i = j;
+      uint64_t local = low_mask();
+      uint64_t blocked = 0;
+      std::vector<size_t> placed;
+      size_t scanned = 0;
+      for (size_t i = first; i < gates.size() && scanned < window_; ++i) {
+        if (done[i]) continue;
+        ++scanned;
+        const Item &it = items[i];
+        if (it.touch & blocked) {
+          blocked |= it.touch;
+          continue;
+        }
+        if (it.wide) {
+          blocked |= it.touch;
+          continue;
+        }
+        if (!it.diag) {
+          const uint64_t nl = local | it.tmask;
+          if (unsigned(__builtin_popcountll(nl)) > L_) {
+            blocked |= it.touch;
+            continue;
+          }
+          local = nl;
+        }
+        placed.push_back(i);
+      }
+      for (size_t i : placed) done[i] = 1;
+      steps.push_back(PlanStep{});
+      PlanStep &st = steps.back();
+      st.is_stage = true;
+      st.ngates = uint32_t(placed.size());
+      build_stage(gates, items, placed, fill_local(local), st.stage);
     }
-    return out;
+    return steps;
   }
 
  private:
-  static uint64_t mask_of(const std::vector<unsigned> &pos) {
-    uint64_t m = 0;
-    for (unsigned p : pos) m |= uint64_t(1) << p;
-    return m;
+  struct Item {
+    bool diag = false;   // diagonal over (targets ∪ controls), at most 6 qubits
+    bool wide = false;   // non-diagonal with more than 2 targets
+    uint64_t tmask = 0;  // target positions
+    uint64_t touch = 0;  // targets ∪ controls
+  };
+
+  uint64_t low_mask() const { return m_ >= 64 ? ~0ull : ((uint64_t(1) << m_) - 1); }
+
+  static bool is_diagonal(const StageGate &g) {
+    const size_t d = size_t(1) << g.pos.size();
+    for (size_t r = 0; r < d; ++r)
+      for (size_t c = 0; c < d; ++c)
+        if (r != c && g.m[r * d + c] != cplx(0., 0.)) return false;
+    return true;
   }
 
-  // Product of gates [i, j) as one matrix over `qubits` (ascending bit
-  // positions), controlled by `shared`.
-  DenseOp compose(const std::vector<StageGate> &gates, size_t i, size_t j, uint64_t qubits,
-                  uint64_t shared) const {
-    DenseOp op;
-    for (unsigned b = 0; b < 64; ++b)
-      if ((qubits >> b) & 1) op.pos.push_back(b);
-    op.ctrl_mask = shared;
-    const size_t K = op.pos.size(), D = size_t(1) << K;
-    auto local = [&](unsigned p) {
-      return unsigned(std::lower_bound(op.pos.begin(), op.pos.end(), p) - op.pos.begin());
-    };
-    if (j - i == 1 && gates[i].ctrl_mask == shared) {
-      // A single gate: keep its own bit order (no composition needed).
-      op.pos = gates[i].pos;
-      op.m = gates[i].m;
+  Item classify(const StageGate &g) const {
+    Item it;
+    for (unsigned p : g.pos) it.tmask |= uint64_t(1) << p;
+    it.touch = it.tmask | g.ctrl_mask;
+    it.diag = is_diagonal(g) && __builtin_popcountll(it.touch) <= 6;
+    it.wide = !it.diag && g.pos.size() > 2;
+    return it;
+  }
+
+  // Complete the local set to exactly L bits with the lowest unused positions.
+  uint64_t fill_local(uint64_t local) const {
+    for (unsigned b = 0; b < nq_ && unsigned(__builtin_popcountll(local)) < L_; ++b) local |= uint64_t(1) << b;
+    return local;
+  }
+
+  struct Op {
+    bool diag;
+    std::vector<unsigned> q;   // dense: target positions (matrix bit order); diag: qubits (ascending)
+    uint64_t ctrl = 0;         // dense only
+    std::vector<cplx> m;       // dense: 2^k x 2^k; diag: 2^k entries
+  };
+
+  static Op to_op(const StageGate &g, const Item &it) {
+    Op op;
+    if (!it.diag) {
+      op.diag = false;
+      op.q = g.pos;
+      op.ctrl = g.ctrl_mask;
+      op.m = g.m;
       return op;
     }
-    std::vector<cplx> M(D * D, cplx(0., 0.)), T(D * D);
-    for (size_t r = 0; r < D; ++r) M[r * D + r] = 1.;
-    for (size_t g = i; g < j; ++g) {
-      const StageGate &G = gates[g];
-      const size_t k = G.pos.size(), d = size_t(1) << k;
-      std::vector<size_t> off(d, 0);
-      size_t tmask = 0;
-      for (size_t l = 0; l < k; ++l) tmask |= size_t(1) << local(G.pos[l]);
-      for (size_t a = 0; a < d; ++a)
-        for (size_t l = 0; l < k; ++l)
-          if ((a >> l) & 1) off[a] |= size_t(1) << local(G.pos[l]);
-      size_t cmask = 0;  // controls folded into the matrix
-      for (unsigned b = 0; b < 64; ++b)
-        if (((G.ctrl_mask & ~shared) >> b) & 1) cmask |= size_t(1) << local(b);
-      T = M;
-      for (size_t r = 0; r < D; ++r) {
-        if (r & tmask) continue;
-        if ((r & cmask) != cmask) continue;  // control not satisfied: identity
-        for (size_t a = 0; a < d; ++a) {
-          cplx *dst = &T[(r + off[a]) * D];
-          for (size_t c = 0; c < D; ++c) dst[c] = 0.;
-          for (size_t b = 0; b < d; ++b) {
-            const cplx w = G.m[a * d + b];
-            if (w == cplx(0., 0.)) continue;
-            const cplx *src = &M[(r + off[b]) * D];
-            for (size_t c = 0; c < D; ++c) dst[c] += w * src[c];
-          }
+    // Diagonal over the ascending set of targets and controls.
+    op.diag = true;
+    for (unsigned b = 0; b < 64; ++b)
+      if ((it.touch >> b) & 1) op.q.push_back(b);
+    const size_t K = op.q.size(), D = size_t(1) << K, d = size_t(1) << g.pos.size();
+    op.m.assign(D, cplx(1., 0.));
+    for (size_t x = 0; x < D; ++x) {
+      bool ctrl_ok = true;
+      size_t local = 0;
+      for (size_t j = 0; j < K; ++j) {
+        const bool bit = (x >> j) & 1;
+        if ((g.ctrl_mask >> op.q[j]) & 1) {
+          if (!bit) ctrl_ok = false;
         }
       }
-      M.swap(T);
+      if (!ctrl_ok) continue;
+      for (size_t l = 0; l < g.pos.size(); ++l) {
+        const size_t j = size_t(std::lower_bound(op.q.begin(), op.q.end(), g.pos[l]) - op.q.begin());
+        if ((x >> j) & 1) local |= size_t(1) << l;
+      }
+      op.m[x] = g.m[local * d + local];
     }
-    op.m = std::move(M);
     return op;
   }
 
-  unsigned nq_;
-  unsigned kmax_;
+  // a <- b * a (b applied after a), both dense on the same targets/controls.
+  static void mul_into(Op &a, const Op &b) {
+    const size_t d = size_t(1) << a.q.size();
+    std::vector<cplx> r(d * d, cplx(0., 0.));
+    for (size_t i = 0; i < d; ++i)
+      for (size_t k = 0; k < d; ++k) {
+        const cplx bik = b.m[i * d + k];
+        if (bik == cplx(0., 0.)) continue;
+        for (size_t j = 0; j < d; ++j) r[i * d + j] += bik * a.m[k * d + j];
+      }
+    a.m.swap(r);
+  }
+
+  // Merge two diagonal ops into one over the union of their qubits.
+  static Op merge_diag(const Op &a, const Op &b) {
+    Op o;
+    o.diag = true;
+    uint64_t u = 0;
+    for (unsigned q : a.q) u |= uint64_t(1) << q;
+    for (unsigned q : b.q) u |= uint64_t(1) << q;
+    for (unsigned x = 0; x < 64; ++x)
+      if ((u >> x) & 1) o.q.push_back(x);
+    const size_t D = size_t(1) << o.q.size();
+    o.m.assign(D, cplx(1., 0.));
+    auto sub = [&](const Op &s, size_t x) {
+      size_t idx = 0;
+      for (size_t j = 0; j < s.q.size(); ++j) {
+        const size_t pj = size_t(std::lower_bound(o.q.begin(), o.q.end(), s.q[j]) - o.q.begin());
+        if ((x >> pj) & 1) idx |= size_t(1) << j;
+      }
+      return s.m[idx];
+    };
+    for (size_t x = 0; x < D; ++x) o.m[x] = sub(b, x) * sub(a, x);
+    return o;
+  }
+
+  static bool same_shape(const Op &a, const Op &b) {
+    return !a.diag && !b.diag && a.q == b.q && a.ctrl == b.ctrl;
+  }
+
+  void build_stage(const std::vector<StageGate> &gates, const std::vector<Item> &items,
+                   const std::vector<size_t> &placed, uint64_t local, StagePlan &sp) const {
+    sp.L = unsigned(__builtin_popcountll(local));
+    sp.lpos.clear();
+    for (unsigned b = 0; b < 64; ++b)
+      if ((local >> b) & 1) sp.lpos.push_back(b);
+    sp.ngates = uint32_t(placed.size());
+    // Operations in order, merged where that changes nothing but rounding.
+    std::vector<Op> ops;
+    for (size_t i : placed) {
+      Op op = to_op(gates[i], items[i]);
+      if (!ops.empty()) {
+        Op &last = ops.back();
+        if (same_shape(last, op)) {
+          mul_into(last, op);
+          continue;
+        }
+        if (last.diag && op.diag) {
+          uint64_t u = 0;
+          for (unsigned q : last.q) u |= uint64_t(1) << q;
+          for (unsigned q : op.q) u |= uint64_t(1) << q;
+          if (__builtin_popcountll(u) <= 6) {
+            last = merge_diag(last, op);
+            continue;
+          }
+        }
+      }
+      ops.push_back(std::move(op));
+    }
+    auto tile_bit = [&](unsigned p) -> int {
+      auto it = std::lower_bound(sp.lpos.begin(), sp.lpos.end(), p);
+      return (it != sp.lpos.end() && *it == p) ? int(it - sp.lpos.begin()) : -1;
+    };
+    sp.ops.clear();
+    sp.pool.clear();
+    for (const Op &op : ops) {
+      StageOpDev d;
+      std::memset(&d, 0, sizeof(d));
+      d.kind = op.diag ? 1 : 0;
+      d.k = uint32_t(op.q.size());
+      d.mat = uint32_t(sp.pool.size());
+      std::memset(d.tbit, 0xFF, sizeof(d.tbit));
+      for (size_t j = 0; j < op.q.size(); ++j) {
+        const int tb = tile_bit(op.q[j]);
+        d.tbit[j] = tb < 0 ? 0xFF : uint8_t(tb);
+        d.gbit[j] = uint8_t(op.q[j]);
+      }
+      if (!op.diag) {
+        for (unsigned b = 0; b < 64; ++b) {
+          if (!((op.ctrl >> b) & 1)) continue;
+          const int tb = tile_bit(b);
+          if (tb >= 0)
+            d.lctrl |= 1u << tb;
+          else
+            d.gctrl |= uint64_t(1) << b;
+        }
+      }
+      sp.pool.insert(sp.pool.end(), op.m.begin(), op.m.end());
+      sp.ops.push_back(d);
+    }
+  }
+
+  unsigned nq_, L_, m_;
+  size_t window_;
 };
 
 }  // namespace gsim

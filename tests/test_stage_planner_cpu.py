@@ -1,0 +1,77 @@
+"""The stage planner (projectq_gb300/csrc/stage.hpp), checked on the CPU.
+
+tests/cpp/stage_plan_check.cpp runs the planner and executes each planned
+stage with the stage kernel's semantics on the host (tile gather by the
+plan's local bit positions, dense operations on tile bits with local and
+non-local controls, diagonal operations over global bits); the result must
+equal the oracle's gate-by-gate application.  This covers the planner's
+look-ahead reordering, operation merging and diagonal conversion."""
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from _backends import make
+from _circuits import allocate, random_mixed_circuit, run_circuit
+from projectq_gb300.workloads import config2_circuit, random_state
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "cpp" / "stage_plan_check.cpp"
+LIB = HERE.parent / "oracle" / "_build" / "libstage_plan_check.so"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    LIB.parent.mkdir(parents=True, exist_ok=True)
+    if not LIB.exists() or LIB.stat().st_mtime < max(SRC.stat().st_mtime,
+                                                     (HERE.parent / "projectq_gb300/csrc/stage.hpp").stat().st_mtime):
+        subprocess.run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", str(SRC), "-o", str(LIB)], check=True)
+    lib = C.CDLL(str(LIB))
+    lib.stage_plan_apply.restype = C.c_int
+    return lib
+
+
+def plan_apply(lib, n, L, m, gates, psi):
+    ks = np.array([len(t) for _, t, _ in gates], dtype=np.uint32)
+    tg = np.array([q for _, t, _ in gates for q in t], dtype=np.uint32)
+    cm = np.array([sum(1 << c for c in cs) for _, _, cs in gates], dtype=np.uint64)
+    mats = np.concatenate([np.ascontiguousarray(m, dtype=np.complex128).reshape(-1) for m, _, _ in gates]).view(np.float64)
+    st = np.ascontiguousarray(psi, dtype=np.complex128).copy()
+    ns = C.c_uint32()
+    P = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
+    lib.stage_plan_apply(C.c_uint(n), C.c_uint(L), C.c_uint(m), C.c_size_t(len(gates)), P(ks, C.c_uint32),
+                         P(tg, C.c_uint32), P(cm, C.c_uint64), P(mats, C.c_double), P(st.view(np.float64), C.c_double),
+                         C.byref(ns))
+    return st, ns.value
+
+
+def oracle_apply(n, gates, psi):
+    o = make("oracle", seed=1)
+    allocate(o, n)
+    o.set_wavefunction(psi, list(range(n)))
+    o.set_fusion("none")
+    run_circuit(o, gates)
+    return o.cheat()[1]
+
+
+@pytest.mark.parametrize("n,L,m,seed", [(9, 6, 3, 0), (10, 7, 4, 1), (11, 8, 5, 2), (6, 6, 3, 3), (12, 12, 5, 4)])
+def test_planned_stages_equal_gate_by_gate(lib, n, L, m, seed):
+    gates = random_mixed_circuit(n, 120, seed, kmax=3, max_ctrl=3)
+    psi = random_state(n, seed=seed)
+    got, nst = plan_apply(lib, n, L, m, gates, psi)
+    exp = oracle_apply(n, gates, psi)
+    assert np.max(np.abs(got - exp)) < 1e-12
+    assert nst >= 1
+
+
+def test_random_circuit_packs_many_gates_per_stage(lib):
+    n = 14
+    gates = config2_circuit(n, depth=10, per_layer=14, seed=3)
+    psi = random_state(n, seed=3)
+    got, nst = plan_apply(lib, n, 11, 5, gates, psi)
+    exp = oracle_apply(n, gates, psi)
+    assert np.max(np.abs(got - exp)) < 1e-12
+    assert len(gates) / nst >= 8  # gates per pass over the state
