@@ -240,6 +240,26 @@ GSIM_API int gsim_profile_clear(gsim_engine *e);
 GSIM_API int gsim_host_register(void *ptr, size_t bytes);
 GSIM_API int gsim_host_unregister(void *ptr);
 
+/* ---- Adjoint-method gradient (no reference counterpart) ---------------------
+ * E(theta) = <psi|H|psi> with psi = U_nops ... U_1 |current state>, and
+ * grad[j] = dE/dtheta_j, by one reverse sweep that un-applies the gates to
+ * psi and to lam = H psi (kernels_adjoint.cu); the engine's state is left
+ * unchanged.  Gate i acts on qubit target[i] with controls
+ * ctrl_ids[ctrl_off[i] .. ctrl_off[i+1]); kind[i]: 0 fixed 2x2 matrix
+ * mats[8i .. 8i+8) (row-major, interleaved re/im), 1 Rx, 2 Ry, 3 Rz, 4 Ph,
+ * 5 R (ProjectQ's matrices) of angle theta[param[i]].  H: Pauli terms with
+ * real coefficients (as gsim_get_expectation_value).  checkpoint_every > 0
+ * stores psi every that many gates on the way forward and reloads it on the
+ * way back (bounds the drift of un-applying gates in complex64). */
+GSIM_API int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *kind,
+                                   const uint32_t *target, const uint32_t *ctrl_off,
+                                   const uint32_t *ctrl_ids, const int32_t *param,
+                                   const double *mats, const double *theta, size_t nparams,
+                                   const uint32_t *term_offsets, const uint32_t *op_qubit,
+                                   const uint8_t *op_pauli, const double *coeffs, size_t nterms,
+                                   const uint32_t *ids, size_t nids, uint32_t checkpoint_every,
+                                   double *energy, double *grad);
+
 /* ---- Allocation-free probability (no counterpart in the reference) ----------
  * Sum of |psi_i|^2 over the indices i with (i & mask) == value, for a state
  * vector the caller owns in device memory (2^nqubits amplitudes of

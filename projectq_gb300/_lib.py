@@ -110,6 +110,11 @@ PRODUCT_ONLY = {
     "profile_clear": (C.c_int, [_eng]),
     "host_register": (C.c_int, [C.c_void_p, _sz]),
     "host_unregister": (C.c_int, [C.c_void_p]),
+    "adjoint_gradient": (
+        C.c_int,
+        [_eng, _sz, _u8p, _u32p, _u32p, _u32p, C.POINTER(C.c_int32), _f64p, _f64p, _sz, _u32p, _u32p, _u8p,
+         _f64p, _sz, _u32p, _sz, C.c_uint32, _f64p, _f64p],
+    ),
     "probability_noalloc": (
         C.c_int,
         [C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, _f64p, C.c_void_p],

@@ -522,6 +522,70 @@ class Engine {
   }
   void synchronize() { CK(cudaStreamSynchronize(stream_)); }
 
+  // ---- adjoint-method gradient (no reference counterpart) -----------------
+  // E = <psi|H|psi> with psi = U(theta) |current state>, and dE/dtheta by one
+  // reverse sweep over psi and lam = H psi, un-applying the gates; psi is
+  // reloaded from checkpoints stored every `ckpt` gates of the forward pass.
+  // The engine's own state is left unchanged.
+  void adjoint(const std::vector<AdjointGate> &gates, const std::vector<int> &param,
+               const std::vector<double> &scale, size_t nparams, const std::vector<PauliTerm> &terms,
+               const std::vector<double> &coeffs, unsigned ckpt, double *energy, double *grad) {
+    run();
+    const size_t n = size_t(1) << N_;
+    void *psi = aux1_.get(n * bpa_);
+    void *lam = aux2_.get(n * bpa_);
+    CK(cudaMemcpyAsync(psi, state_.p, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
+    std::vector<DevBuf> ck;
+    std::vector<int> ck_at(gates.size(), -1);  // checkpoint index holding the state after gate i
+    for (size_t i = 0; i < gates.size(); ++i) {
+      DenseOp op;
+      op.m.assign(gates[i].u, gates[i].u + 4);
+      op.pos = {gates[i].target};
+      op.ctrl_mask = gates[i].ctrl_mask;
+      CK(launch_dense(prec_, psi, N_, op, stream_));
+      if (ckpt && (i + 1) % ckpt == 0 && i + 1 < gates.size()) {
+        ck.emplace_back();
+        void *c = ck.back().get(n * bpa_);
+        CK(cudaMemcpyAsync(c, psi, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
+        ck_at[i] = int(ck.size()) - 1;
+      }
+    }
+    std::vector<PauliApplyTermDev> dev(terms.size());
+    for (size_t t = 0; t < terms.size(); ++t) dev[t] = apply_term_dev(terms[t], cplx(coeffs[t], 0.));
+    auto *d_terms = static_cast<PauliApplyTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliApplyTermDev)));
+    if (!dev.empty())
+      CK(cudaMemcpyAsync(d_terms, dev.data(), dev.size() * sizeof(dev[0]), cudaMemcpyHostToDevice, stream_));
+    CK(launch_pauli_apply(prec_, psi, lam, N_, d_terms, int(dev.size()), stream_));
+    double *d_out = static_cast<double *>(small_.get(4096));
+    CK(launch_compare(prec_, psi, prec_, lam, n, part(), d_out, stream_));
+    double e3[3];
+    CK(cudaMemcpyAsync(e3, d_out, 24, cudaMemcpyDeviceToHost, stream_));
+    const int nblk = adjoint_blocks(N_);
+    size_t ncols = 0;
+    for (int p : param) ncols += p >= 0;
+    auto *d_part = static_cast<double *>(table_.get(std::max<size_t>(1, ncols) * nblk * 8));
+    std::vector<int> col(gates.size(), -1);
+    int c = 0;
+    for (size_t i = gates.size(); i-- > 0;) {
+      if (param[i] >= 0) col[i] = c++;
+      CK(launch_adjoint_step(prec_, psi, lam, N_, gates[i], col[i], d_part, nblk, stream_));
+      if (i > 0 && ck_at[i - 1] >= 0)
+        CK(cudaMemcpyAsync(psi, ck[ck_at[i - 1]].p, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
+    }
+    std::vector<double> g(ncols);
+    if (ncols) {
+      auto *d_g = static_cast<double *>(table2_.get(ncols * 8));
+      CK(launch_column_sums(d_part, nblk, int(ncols), d_g, stream_));
+      CK(cudaMemcpyAsync(g.data(), d_g, ncols * 8, cudaMemcpyDeviceToHost, stream_));
+    }
+    CK(cudaStreamSynchronize(stream_));
+    for (auto &b : ck) b.release();
+    *energy = e3[0];
+    std::fill(grad, grad + nparams, 0.);
+    for (size_t i = 0; i < gates.size(); ++i)
+      if (param[i] >= 0) grad[param[i]] += scale[i] * g[col[i]];
+  }
+
   // <this|other>, max |this_i - other_i| (no reference counterpart).
   void compare(Engine &other, double *out) {
     run();
@@ -777,6 +841,7 @@ class Engine {
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
   unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
+  bool use_reg_stages_ = true;
   DevBuf upload_dev_;
   HostBuf upload_host_;
   cudaEvent_t upload_ev_ = nullptr;
@@ -917,16 +982,24 @@ void Engine::run_staged() {
   const unsigned m = prec_ == GSIM_C64 ? 5 : 4;
   StagePlanner planner(N_, L, m);
   std::vector<PlanStep> steps = planner.plan(gates);
+  // Register substages where the tile is 2^(r + 8) amplitudes (256 threads).
+  const unsigned r = prec_ == GSIM_C64 ? 4 : 3, rho = prec_ == GSIM_C64 ? 4 : 3;
+  for (auto &st : steps)
+    if (st.is_stage && use_reg_stages_ && st.stage.L == r + 8) build_substages(st.stage, r, rho);
   // Serialise every stage's operations and matrices into one upload.
   const size_t esz = bpa_;
   size_t bytes = 0;
   std::vector<size_t> off_ops(steps.size()), off_pool(steps.size());
   for (size_t i = 0; i < steps.size(); ++i) {
     if (!steps[i].is_stage) continue;
+    const StagePlan &sp = steps[i].stage;
     off_ops[i] = bytes;
-    bytes += (steps[i].stage.ops.size() * sizeof(StageOpDev) + 15) / 16 * 16;
+    if (!sp.subs.empty())
+      bytes += stage_subs_bytes(sp) + (sp.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16;
+    else
+      bytes += (sp.ops.size() * sizeof(StageOpDev) + 15) / 16 * 16;
     off_pool[i] = bytes;
-    bytes += (steps[i].stage.pool.size() * esz + 15) / 16 * 16;
+    bytes += (sp.pool.size() * esz + 15) / 16 * 16;
   }
   char *dev = nullptr;
   if (bytes) {
@@ -935,7 +1008,12 @@ void Engine::run_staged() {
     for (size_t i = 0; i < steps.size(); ++i) {
       if (!steps[i].is_stage) continue;
       const StagePlan &sp = steps[i].stage;
-      std::memcpy(host + off_ops[i], sp.ops.data(), sp.ops.size() * sizeof(StageOpDev));
+      if (!sp.subs.empty()) {
+        std::memcpy(host + off_ops[i], sp.subs.data(), sp.subs.size() * sizeof(SubstageDev));
+        std::memcpy(host + off_ops[i] + stage_subs_bytes(sp), sp.sops.data(), sp.sops.size() * sizeof(SubOpDev));
+      } else {
+        std::memcpy(host + off_ops[i], sp.ops.data(), sp.ops.size() * sizeof(StageOpDev));
+      }
       if (prec_ == GSIM_C64) {
         float *f = reinterpret_cast<float *>(host + off_pool[i]);
         for (size_t j = 0; j < sp.pool.size(); ++j) {
@@ -1283,6 +1361,68 @@ int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n) {
 }
 int gsim_reset_counters(gsim_engine *e) {
   return guard([&] { E(e)->reset_counters(); });
+}
+int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *kind, const uint32_t *target,
+                          const uint32_t *ctrl_off, const uint32_t *ctrl_ids, const int32_t *param,
+                          const double *mats, const double *theta, size_t nparams,
+                          const uint32_t *term_offsets, const uint32_t *op_qubit, const uint8_t *op_pauli,
+                          const double *coeffs, size_t nterms, const uint32_t *ids, size_t nids,
+                          uint32_t checkpoint_every, double *energy, double *grad) {
+  return guard([&] {
+    Engine *eng = E(e);
+    eng->run();
+    const auto &m = eng->mapping();
+    auto pos = [&](uint32_t id) {
+      auto it = m.find(id);
+      if (it == m.end()) fail(GSIM_ERR_RUNTIME, "adjoint_gradient(): unknown qubit id " + std::to_string(id));
+      return it->second;
+    };
+    std::vector<gsim::AdjointGate> gates(nops);
+    std::vector<int> prm(nops, -1);
+    std::vector<double> scale(nops, 0.);
+    using gsim::cplx;
+    const cplx I(0., 1.);
+    for (size_t i = 0; i < nops; ++i) {
+      gsim::AdjointGate &g = gates[i];
+      g.target = pos(target[i]);
+      for (uint32_t c = ctrl_off[i]; c < ctrl_off[i + 1]; ++c) {
+        const unsigned p = pos(ctrl_ids[c]);
+        if (p == g.target) fail(GSIM_ERR_VALUE, "adjoint_gradient(): a control is also the target");
+        g.ctrl_mask |= uint64_t(1) << p;
+      }
+      if (kind[i] == 0) {
+        for (int j = 0; j < 4; ++j) g.u[j] = cplx(mats[8 * i + 2 * j], mats[8 * i + 2 * j + 1]);
+        continue;
+      }
+      if (param[i] < 0 || size_t(param[i]) >= nparams)
+        fail(GSIM_ERR_VALUE, "adjoint_gradient(): parameter index out of range");
+      prm[i] = param[i];
+      const double t = theta[param[i]], c = std::cos(0.5 * t), s = std::sin(0.5 * t);
+      switch (kind[i]) {
+        case 1:  // Rx (projectq/ops/_gates.py:276-281)
+          g.u[0] = c; g.u[1] = -I * s; g.u[2] = -I * s; g.u[3] = c; g.gen = 0; scale[i] = 1.;
+          break;
+        case 2:  // Ry (:290-295)
+          g.u[0] = c; g.u[1] = -s; g.u[2] = s; g.u[3] = c; g.gen = 1; scale[i] = 1.;
+          break;
+        case 3:  // Rz (:304-309)
+          g.u[0] = std::exp(-0.5 * I * t); g.u[1] = 0.; g.u[2] = 0.; g.u[3] = std::exp(0.5 * I * t);
+          g.gen = 2; scale[i] = 1.;
+          break;
+        case 4:  // Ph (:267)
+          g.u[0] = std::exp(I * t); g.u[1] = 0.; g.u[2] = 0.; g.u[3] = std::exp(I * t); g.gen = 3; scale[i] = -2.;
+          break;
+        case 5:  // R (diag(1, e^{i t}))
+          g.u[0] = 1.; g.u[1] = 0.; g.u[2] = 0.; g.u[3] = std::exp(I * t); g.gen = 4; scale[i] = -2.;
+          break;
+        default:
+          fail(GSIM_ERR_VALUE, "adjoint_gradient(): unknown gate kind");
+      }
+    }
+    auto terms = terms_of(eng, term_offsets, op_qubit, op_pauli, nterms, ids, nids);
+    eng->adjoint(gates, prm, scale, nparams, terms, std::vector<double>(coeffs, coeffs + nterms),
+                 checkpoint_every, energy, grad);
+  });
 }
 int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out) {
   return guard([&] { E(a)->compare(*E(b), out); });

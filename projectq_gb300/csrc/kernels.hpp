@@ -110,4 +110,18 @@ cudaError_t launch_math_scatter(int prec, const void *in, void *out, unsigned nq
 cudaError_t launch_compare(int prec_a, const void *a, int prec_b, const void *b, uint64_t n,
                            double *d_part, double *d_out, cudaStream_t s);
 
+// Adjoint gradient: one reverse-sweep step over (psi, lam) for a 1-target gate
+// u (2x2 row-major, FP64) with controls; gen selects the generator whose
+// Im<lam|Pi_c G|psi> is reduced into column `col` of d_part (-1: none;
+// 0 X, 1 Y, 2 Z, 3 identity, 4 |1><1|).
+struct AdjointGate {
+  cplx u[4];
+  unsigned target = 0;
+  uint64_t ctrl_mask = 0;
+  int gen = -1;
+};
+int adjoint_blocks(unsigned nq);
+cudaError_t launch_adjoint_step(int prec, void *psi, void *lam, unsigned nq, const AdjointGate &g,
+                                int col, double *d_part, int nblk, cudaStream_t s);
+
 }  // namespace gsim

@@ -164,6 +164,186 @@ __global__ void __launch_bounds__(256) stage_kernel(cplx_t<T> *__restrict__ psi,
   }
 }
 
+// ---- register substages (stage.hpp: build_substages) ----------------------
+__device__ __forceinline__ uint32_t swz(uint32_t p, uint32_t rho) {
+  uint32_t x = p >> rho, f = 0;
+  const uint32_t mask = (1u << rho) - 1;
+#pragma unroll 1
+  while (x) {
+    f ^= x & mask;
+    x >>= rho;
+  }
+  return p ^ f;
+}
+
+template <typename T>
+__device__ __forceinline__ void cmac_k(int kd, cplx_t<T> m, cplx_t<T> v, T &re, T &im) {
+  if (kd & 1) {
+    re = fma(m.x, v.x, re);
+    im = fma(m.x, v.y, im);
+  }
+  if (kd & 2) {
+    re = fma(-m.y, v.y, re);
+    im = fma(m.y, v.x, im);
+  }
+}
+
+template <typename T, int R, int B>
+__device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+  const cplx_t<T> m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
+  const int k0 = op.ek[0], k1 = op.ek[1], k2 = op.ek[2], k3 = op.ek[3];
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) {
+    if ((j >> B) & 1) continue;
+    if ((uint32_t(j) & op.jctrl) != op.jctrl) continue;
+    const cplx_t<T> a = v[j], b = v[j | (1 << B)];
+    T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
+    cmac_k<T>(k0, m00, a, r0, i0);
+    cmac_k<T>(k1, m01, b, r0, i0);
+    cmac_k<T>(k2, m10, a, r1, i1);
+    cmac_k<T>(k3, m11, b, r1, i1);
+    v[j] = mkc<T>(r0, i0);
+    v[j | (1 << B)] = mkc<T>(r1, i1);
+  }
+}
+
+template <typename T, int R, int B0, int B1>
+__device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+  cplx_t<T> mm[16];
+#pragma unroll
+  for (int e = 0; e < 16; ++e) mm[e] = M[e];
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) {
+    if (((j >> B0) & 1) || ((j >> B1) & 1)) continue;
+    if ((uint32_t(j) & op.jctrl) != op.jctrl) continue;
+    const int j1 = j | (1 << B0), j2 = j | (1 << B1), j3 = j1 | (1 << B1);
+    const cplx_t<T> x[4] = {v[j], v[j1], v[j2], v[j3]};
+    cplx_t<T> y[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      T re = T(0), im = T(0);
+#pragma unroll
+      for (int b = 0; b < 4; ++b) cfma<T>(mm[a * 4 + b], x[b], re, im);
+      y[a] = mkc<T>(re, im);
+    }
+    v[j] = y[0];
+    v[j1] = y[1];
+    v[j2] = y[2];
+    v[j3] = y[3];
+  }
+}
+
+template <typename T, int R>
+__device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M,
+                                          uint32_t row, uint64_t base) {
+  if (op.kind == 2) {
+    uint32_t cidx = 0;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      if (q >= int(op.dk)) break;
+      if (op.dloc[q] == 1) cidx |= ((row >> op.didx[q]) & 1u) << q;
+      else if (op.dloc[q] == 2) cidx |= uint32_t((base >> op.didx[q]) & 1) << q;
+    }
+#pragma unroll
+    for (int j = 0; j < (1 << R); ++j) {
+      uint32_t idx = cidx;
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (q >= int(op.dk)) break;
+        if (op.dloc[q] == 0) idx |= ((uint32_t(j) >> op.didx[q]) & 1u) << q;
+      }
+      v[j] = cmul<T>(v[j], M[idx]);
+    }
+    return;
+  }
+  if (op.kind == 0) {
+    switch (op.rb[0]) {
+      case 0: reg_dense1<T, R, 0>(v, op, M); break;
+      case 1: if constexpr (R > 1) reg_dense1<T, R, 1>(v, op, M); break;
+      case 2: if constexpr (R > 2) reg_dense1<T, R, 2>(v, op, M); break;
+      case 3: if constexpr (R > 3) reg_dense1<T, R, 3>(v, op, M); break;
+    }
+    return;
+  }
+  const int key = op.rb[0] * 4 + op.rb[1];
+#define GSIM_D2(a, b) \
+  case a * 4 + b:     \
+    if constexpr (R > a && R > b) reg_dense2<T, R, a, b>(v, op, M); \
+    break;
+  switch (key) {
+    GSIM_D2(0, 1) GSIM_D2(1, 0) GSIM_D2(0, 2) GSIM_D2(2, 0) GSIM_D2(0, 3) GSIM_D2(3, 0)
+    GSIM_D2(1, 2) GSIM_D2(2, 1) GSIM_D2(1, 3) GSIM_D2(3, 1) GSIM_D2(2, 3) GSIM_D2(3, 2)
+  }
+#undef GSIM_D2
+}
+
+template <typename T, int R>
+__global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
+                                                        const SubstageDev *__restrict__ subs, int nsubs,
+                                                        const SubOpDev *__restrict__ ops,
+                                                        const cplx_t<T> *__restrict__ pool, uint32_t rho) {
+  using C = cplx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const uint32_t TS = 1u << A.L;
+  C *tile = reinterpret_cast<C *>(smem);
+  uint64_t *segoff = reinterpret_cast<uint64_t *>(smem + size_t(TS) * sizeof(C));
+  const uint32_t nseg = 1u << A.h;
+  for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
+    uint64_t o = 0;
+    for (uint32_t b = 0; b < A.h; ++b)
+      if ((s >> b) & 1) o |= uint64_t(1) << A.lpos[A.m + b];
+    segoff[s] = o;
+  }
+  __syncthreads();
+  const uint32_t row = threadIdx.x;
+  const uint32_t mask = (1u << A.m) - 1;
+  for (uint64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const uint64_t base = insert_zeros(t, A.lpos, int(A.L));
+    if constexpr (sizeof(T) == 4) {
+      for (uint32_t v2 = threadIdx.x; v2 < (TS >> 1); v2 += blockDim.x) {
+        const uint32_t p = v2 << 1;
+        const float4 x = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p >> A.m] + (p & mask)));
+        tile[swz(p, rho)] = make_float2(x.x, x.y);
+        tile[swz(p + 1, rho)] = make_float2(x.z, x.w);
+      }
+    } else {
+      for (uint32_t p = threadIdx.x; p < TS; p += blockDim.x)
+        tile[swz(p, rho)] = __ldcs(psi + base + segoff[p >> A.m] + (p & mask));
+    }
+    __syncthreads();
+    for (int si = 0; si < nsubs; ++si) {
+      const SubstageDev &S = subs[si];
+      uint32_t srow = 0;
+#pragma unroll
+      for (int b = 0; b < 8; ++b)
+        if ((row >> b) & 1) srow ^= S.rowsw[b];
+      C v[1 << R];
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) v[j] = tile[srow ^ S.soff[j]];
+      for (uint32_t o = S.op_begin; o < S.op_end; ++o) {
+        const SubOpDev op = ops[o];
+        if ((base & op.gctrl) != op.gctrl) continue;
+        if ((row & op.tctrl) != op.tctrl) continue;
+        reg_apply<T, R>(v, op, pool + op.mat, row, base);
+      }
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) tile[srow ^ S.soff[j]] = v[j];
+      __syncthreads();
+    }
+    if constexpr (sizeof(T) == 4) {
+      for (uint32_t v2 = threadIdx.x; v2 < (TS >> 1); v2 += blockDim.x) {
+        const uint32_t p = v2 << 1;
+        const float2 a = tile[swz(p, rho)], b = tile[swz(p + 1, rho)];
+        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & mask)), make_float4(a.x, a.y, b.x, b.y));
+      }
+    } else {
+      for (uint32_t p = threadIdx.x; p < TS; p += blockDim.x)
+        __stcs(psi + base + segoff[p >> A.m] + (p & mask), tile[swz(p, rho)]);
+    }
+    __syncthreads();
+  }
+}
+
 int stage_sms() {
   static int n = 0;
   if (!n) {
@@ -193,6 +373,27 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
   if (!attr_set) {
     cudaFuncSetAttribute(stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
     attr_set = true;
+  }
+  if (!plan.subs.empty()) {
+    // Register substages: d_ops holds the SubstageDev array, then the SubOpDev array.
+    constexpr int R = sizeof(T) == 4 ? 4 : 3;
+    if (plan.r != unsigned(R) || plan.L != unsigned(R) + 8) return cudaErrorInvalidValue;
+    static bool reg_attr = false;
+    if (!reg_attr) {
+      cudaFuncSetAttribute(stage_reg_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+      reg_attr = true;
+    }
+    int per_sm = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_reg_kernel<T, R>, 256, smem);
+    per_sm = std::max(1, per_sm);
+    const uint64_t grid = std::min<uint64_t>(A.ntiles, uint64_t(stage_sms()) * per_sm);
+    const auto *subs = static_cast<const SubstageDev *>(d_ops);
+    const auto *sops = reinterpret_cast<const SubOpDev *>(static_cast<const char *>(d_ops) +
+                                                          stage_subs_bytes(plan));
+    stage_reg_kernel<T, R><<<unsigned(grid), 256, smem, s>>>(static_cast<cplx_t<T> *>(psi), A, subs,
+                                                             int(plan.subs.size()), sops,
+                                                             static_cast<const cplx_t<T> *>(d_pool), plan.rho);
+    return cudaGetLastError();
   }
   int per_sm = 1;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_kernel<T>, 256, smem);

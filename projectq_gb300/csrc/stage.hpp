@@ -53,13 +53,171 @@ struct StageOpDev {
   uint8_t gbit[8];   // global bit position of diagonal qubit j
 };
 
+// Register substages.  The register kernel gives each of its 256 threads
+// 2^r amplitudes of the tile in registers: the thread's "row" (a value of
+// the L - r row bits) times every value of the r register bits R.  A
+// substage is a run of the stage's operations whose dense targets all lie in
+// R; it costs one shared-memory round trip however many operations it holds.
+// Diagonal operations join any substage.  Shared memory holds the tile in a
+// swizzled order s(p) = p ^ fold(p >> rho), fold XOR-ing rho-bit chunks, so
+// tile bit b lands in bank class b mod rho; the five lane bits are chosen to
+// cover every class, which makes each register access conflict-free.
+struct SubOpDev {
+  uint32_t kind;    // 0 dense 1-qubit, 1 dense 2-qubit, 2 diagonal
+  uint32_t mat;     // offset in the stage's pool
+  uint32_t jctrl;   // controls among the register bits (mask over j)
+  uint32_t tctrl;   // controls among the row bits (mask over the row index)
+  uint64_t gctrl;   // non-local controls (global mask)
+  uint8_t rb[2];    // dense: register-bit index of matrix bit 0 / 1
+  uint8_t ek[4];    // dense 1-qubit: kinds of m00 m01 m10 m11 (0 zero, 1 real, 2 imag, 3 complex)
+  uint8_t dk;       // diagonal: number of qubits
+  uint8_t dloc[6];  // diagonal qubit q: 0 register bit, 1 row bit, 2 non-local
+  uint8_t didx[6];  //   its register-bit index / row-bit index / global bit position
+  uint8_t pad[3];
+};
+struct SubstageDev {
+  uint32_t op_begin, op_end;
+  uint32_t soff[16];   // swizzled offset of register index j (XOR with the row's offset)
+  uint32_t rowsw[16];  // swizzled offset of row bit i; a row's offset is the XOR of its set bits
+};
+
 struct StagePlan {
   unsigned L = 0;                 // tile bits
   std::vector<unsigned> lpos;     // ascending global positions of the tile bits (lpos[i] = i for i < m)
   std::vector<StageOpDev> ops;
   std::vector<cplx> pool;         // matrices / diagonals, FP64 (converted at upload)
   uint32_t ngates = 0;            // logical gates applied
+  unsigned r = 0, rho = 0;        // register bits and bank-class bits (0: no register substages)
+  std::vector<SubstageDev> subs;
+  std::vector<SubOpDev> sops;
 };
+
+// Bytes of the SubstageDev array as uploaded (the SubOpDev array follows it).
+inline size_t stage_subs_bytes(const StagePlan &sp) {
+  return (sp.subs.size() * sizeof(SubstageDev) + 15) / 16 * 16;
+}
+
+// s(p) = p ^ fold(p >> rho): fold XORs the rho-bit chunks of its argument.
+inline uint32_t tile_swizzle(uint32_t p, unsigned rho) {
+  uint32_t x = p >> rho, f = 0;
+  const uint32_t mask = (1u << rho) - 1;
+  while (x) {
+    f ^= x & mask;
+    x >>= rho;
+  }
+  return p ^ f;
+}
+
+// Split sp.ops into register substages of r register bits (256 threads:
+// sp.L == r + 8).  Entry kinds let 1-qubit operations skip zero entries.
+inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
+  sp.r = r;
+  sp.rho = rho;
+  sp.subs.clear();
+  sp.sops.clear();
+  const unsigned L = sp.L;
+  size_t i = 0;
+  while (i < sp.ops.size()) {
+    uint32_t R = 0;  // tile-bit mask
+    size_t j = i;
+    for (; j < sp.ops.size(); ++j) {
+      const StageOpDev &op = sp.ops[j];
+      if (op.kind == 1) continue;
+      uint32_t T = 0;
+      for (unsigned q = 0; q < op.k; ++q) T |= 1u << op.tbit[q];
+      if (unsigned(__builtin_popcount(R | T)) > r) break;
+      R |= T;
+    }
+    // Pad R to r bits, taking bits from the bank classes with most spare bits.
+    while (unsigned(__builtin_popcount(R)) < r) {
+      int best = -1, best_count = -1;
+      for (unsigned b = 0; b < L; ++b) {
+        if ((R >> b) & 1) continue;
+        int cnt = 0;
+        for (unsigned c = 0; c < L; ++c)
+          if (!((R >> c) & 1) && c % rho == b % rho) ++cnt;
+        if (cnt > best_count) {
+          best_count = cnt;
+          best = int(b);
+        }
+      }
+      R |= 1u << best;
+    }
+    // Register bits ascending; row bits: one per bank class first (lanes).
+    std::vector<unsigned> rbits, rows, rest;
+    for (unsigned b = 0; b < L; ++b)
+      if ((R >> b) & 1) rbits.push_back(b);
+    std::vector<char> cls(rho, 0);
+    for (unsigned b = 0; b < L; ++b) {
+      if ((R >> b) & 1) continue;
+      if (!cls[b % rho] && rows.size() < 5) {
+        cls[b % rho] = 1;
+        rows.push_back(b);
+      } else {
+        rest.push_back(b);
+      }
+    }
+    for (unsigned b : rest) rows.push_back(b);
+    SubstageDev sd;
+    std::memset(&sd, 0, sizeof(sd));
+    sd.op_begin = uint32_t(sp.sops.size());
+    for (uint32_t x = 0; x < (1u << r); ++x) {
+      uint32_t pos = 0;
+      for (unsigned q = 0; q < r; ++q)
+        if ((x >> q) & 1) pos |= 1u << rbits[q];
+      sd.soff[x] = tile_swizzle(pos, rho);
+    }
+    for (size_t q = 0; q < rows.size(); ++q) sd.rowsw[q] = tile_swizzle(1u << rows[q], rho);
+    auto reg_index = [&](unsigned tb) {
+      return int(std::find(rbits.begin(), rbits.end(), tb) - rbits.begin());
+    };
+    auto row_index = [&](unsigned tb) {
+      return int(std::find(rows.begin(), rows.end(), tb) - rows.begin());
+    };
+    for (size_t o = i; o < j; ++o) {
+      const StageOpDev &op = sp.ops[o];
+      SubOpDev so;
+      std::memset(&so, 0, sizeof(so));
+      so.mat = op.mat;
+      so.gctrl = op.gctrl;
+      for (unsigned b = 0; b < L; ++b) {
+        if (!((op.lctrl >> b) & 1)) continue;
+        if ((R >> b) & 1)
+          so.jctrl |= 1u << reg_index(b);
+        else
+          so.tctrl |= 1u << row_index(b);
+      }
+      if (op.kind == 1) {
+        so.kind = 2;
+        so.dk = uint8_t(op.k);
+        for (unsigned q = 0; q < op.k; ++q) {
+          if (op.tbit[q] == 0xFF) {
+            so.dloc[q] = 2;
+            so.didx[q] = op.gbit[q];
+          } else if ((R >> op.tbit[q]) & 1) {
+            so.dloc[q] = 0;
+            so.didx[q] = uint8_t(reg_index(op.tbit[q]));
+          } else {
+            so.dloc[q] = 1;
+            so.didx[q] = uint8_t(row_index(op.tbit[q]));
+          }
+        }
+      } else {
+        so.kind = op.k == 1 ? 0 : 1;
+        for (unsigned q = 0; q < op.k; ++q) so.rb[q] = uint8_t(reg_index(op.tbit[q]));
+        if (op.k == 1)
+          for (int e = 0; e < 4; ++e) {
+            const cplx z = sp.pool[op.mat + e];
+            so.ek[e] = uint8_t((z.real() != 0. ? 1 : 0) | (z.imag() != 0. ? 2 : 0));
+          }
+      }
+      sp.sops.push_back(so);
+    }
+    sd.op_end = uint32_t(sp.sops.size());
+    sp.subs.push_back(sd);
+    i = j;
+  }
+}
 
 // One step of the plan: either a stage or a single wide dense gate.
 struct PlanStep {

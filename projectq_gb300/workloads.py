@@ -118,3 +118,17 @@ def mt19937_uniform(seed, count):
             r = math.nextafter(1.0, 0.0)
         out.append(r)
     return out
+
+
+def random_pauli_hamiltonian(n, nterms=200, seed=0, p_identity=0.7):
+    """`nterms` Pauli strings: each qubit I with probability p_identity and
+    X, Y, Z with (1 - p_identity)/3 each; coefficients ~ N(0, 1).  Returned
+    as [(term, coeff)] with term = [(qubit index, 'X'|'Y'|'Z'), ...]."""
+    rng = np.random.default_rng(seed)
+    q = (1.0 - p_identity) / 3.0
+    terms = []
+    for _ in range(nterms):
+        ops = rng.choice(4, size=n, p=[p_identity, q, q, q])
+        term = [(i, "XYZ"[o - 1]) for i, o in enumerate(ops) if o]
+        terms.append((term, float(rng.standard_normal())))
+    return terms

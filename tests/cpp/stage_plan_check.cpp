@@ -81,9 +81,77 @@ void apply_stage(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &sp)
   }
 }
 
+// The register kernel's semantics: the tile in swizzled order, each substage
+// loading 2^r amplitudes per row into "registers", applying its operations
+// with register / row / non-local controls, and storing them back.
+void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &sp) {
+  const unsigned L = sp.L, r = sp.r;
+  const size_t TS = size_t(1) << L, ntiles = size_t(1) << (nq - L), nrows = TS >> r;
+  std::vector<cplx> smem(TS);
+  for (size_t t = 0; t < ntiles; ++t) {
+    size_t base = t;
+    for (unsigned p : sp.lpos) base = ((base >> p) << (p + 1)) | (base & ((size_t(1) << p) - 1));
+    auto gidx = [&](size_t p) {
+      size_t g = base;
+      for (unsigned b = 0; b < L; ++b)
+        if ((p >> b) & 1) g |= size_t(1) << sp.lpos[b];
+      return g;
+    };
+    for (size_t p = 0; p < TS; ++p) smem[gsim::tile_swizzle(uint32_t(p), sp.rho)] = psi[gidx(p)];
+    for (auto const &S : sp.subs) {
+      for (uint32_t row = 0; row < nrows; ++row) {
+        uint32_t srow = 0;
+        for (unsigned b = 0; b < L - r; ++b)
+          if ((row >> b) & 1) srow ^= S.rowsw[b];
+        std::vector<cplx> v(size_t(1) << r);
+        for (uint32_t j = 0; j < v.size(); ++j) v[j] = smem[srow ^ S.soff[j]];
+        for (uint32_t o = S.op_begin; o < S.op_end; ++o) {
+          const gsim::SubOpDev &op = sp.sops[o];
+          if ((base & op.gctrl) != op.gctrl) continue;
+          if ((row & op.tctrl) != op.tctrl) continue;
+          const cplx *M = sp.pool.data() + op.mat;
+          if (op.kind == 2) {
+            for (uint32_t j = 0; j < v.size(); ++j) {
+              uint32_t idx = 0;
+              for (unsigned q = 0; q < op.dk; ++q) {
+                uint32_t bit = op.dloc[q] == 0 ? (j >> op.didx[q]) & 1
+                               : op.dloc[q] == 1 ? (row >> op.didx[q]) & 1
+                                                 : uint32_t((base >> op.didx[q]) & 1);
+                idx |= bit << q;
+              }
+              v[j] *= M[idx];
+            }
+          } else {
+            const unsigned k = op.kind == 0 ? 1 : 2, d = 1u << k;
+            uint32_t tm = 0;
+            for (unsigned q = 0; q < k; ++q) tm |= 1u << op.rb[q];
+            for (uint32_t j = 0; j < v.size(); ++j) {
+              if ((j & tm) || (j & op.jctrl) != op.jctrl) continue;
+              std::vector<uint32_t> jj(d);
+              for (uint32_t a = 0; a < d; ++a) {
+                jj[a] = j;
+                for (unsigned q = 0; q < k; ++q)
+                  if ((a >> q) & 1) jj[a] |= 1u << op.rb[q];
+              }
+              std::vector<cplx> x(d), y(d, 0.);
+              for (uint32_t a = 0; a < d; ++a) x[a] = v[jj[a]];
+              for (uint32_t a = 0; a < d; ++a)
+                for (uint32_t b = 0; b < d; ++b) y[a] += M[a * d + b] * x[b];
+              for (uint32_t a = 0; a < d; ++a) v[jj[a]] = y[a];
+            }
+          }
+        }
+        for (uint32_t j = 0; j < v.size(); ++j) smem[srow ^ S.soff[j]] = v[j];
+      }
+    }
+    for (size_t p = 0; p < TS; ++p) psi[gidx(p)] = smem[gsim::tile_swizzle(uint32_t(p), sp.rho)];
+  }
+}
+
 }  // namespace
 
-extern "C" int stage_plan_apply(unsigned nq, unsigned L, unsigned m, size_t ngates, const uint32_t *ks,
+extern "C" int stage_plan_apply(unsigned nq, unsigned L, unsigned m, unsigned r, unsigned rho, size_t ngates,
+                                const uint32_t *ks,
                                 const uint32_t *targets, const uint64_t *ctrl_masks, const double *mats,
                                 double *state, uint32_t *nstages_out) {
   std::vector<gsim::StageGate> gates(ngates);
@@ -100,9 +168,14 @@ extern "C" int stage_plan_apply(unsigned nq, unsigned L, unsigned m, size_t ngat
   std::vector<cplx> psi(size_t(1) << nq);
   for (size_t i = 0; i < psi.size(); ++i) psi[i] = cplx(state[2 * i], state[2 * i + 1]);
   uint32_t ns = 0;
-  for (auto const &st : steps) {
+  for (auto &st : steps) {
     if (st.is_stage) {
-      apply_stage(psi, nq, st.stage);
+      if (r > 0 && st.stage.L > r) {
+        gsim::build_substages(st.stage, r, rho);
+        apply_stage_substages(psi, nq, st.stage);
+      } else {
+        apply_stage(psi, nq, st.stage);
+      }
       ++ns;
     } else {
       apply_dense(psi, nq, st.dense);

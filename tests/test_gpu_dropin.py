@@ -30,10 +30,12 @@ def test_reference_suite_complex128(fusion):
 def test_reference_suite_complex64():
     """complex64 storage: the reference's default pytest.approx tolerances
     (rel 1e-6, abs 1e-12) hold except where a test compares an amplitude that
-    should be exactly zero with abs=1e-12; those are listed here."""
+    should be exactly zero against an absolute threshold below complex64's
+    rounding (abs=1e-12 in functional_entangle; |a| > 1e-8 after H.H in
+    test_factoring, where complex64 leaves ~3e-8); those are listed here."""
     rc, passed, out = _refsuite.run("gpu", "c64", "staged")
     failed = [line for line in out.splitlines() if line.startswith("FAILED")]
-    allowed = ("test_simulator_functional_entangle", "test_simulator_time_evolution")
+    allowed = ("test_simulator_functional_entangle", "test_simulator_time_evolution", "test_factoring")
     unexpected = [f for f in failed if not any(a in f for a in allowed)]
     assert not unexpected, out[-6000:]
     assert passed >= 50

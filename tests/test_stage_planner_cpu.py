@@ -34,7 +34,7 @@ def lib():
     return lib
 
 
-def plan_apply(lib, n, L, m, gates, psi):
+def plan_apply(lib, n, L, m, gates, psi, r=0, rho=4):
     ks = np.array([len(t) for _, t, _ in gates], dtype=np.uint32)
     tg = np.array([q for _, t, _ in gates for q in t], dtype=np.uint32)
     cm = np.array([sum(1 << c for c in cs) for _, _, cs in gates], dtype=np.uint64)
@@ -42,7 +42,8 @@ def plan_apply(lib, n, L, m, gates, psi):
     st = np.ascontiguousarray(psi, dtype=np.complex128).copy()
     ns = C.c_uint32()
     P = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
-    lib.stage_plan_apply(C.c_uint(n), C.c_uint(L), C.c_uint(m), C.c_size_t(len(gates)), P(ks, C.c_uint32),
+    lib.stage_plan_apply(C.c_uint(n), C.c_uint(L), C.c_uint(m), C.c_uint(r), C.c_uint(rho), C.c_size_t(len(gates)),
+                         P(ks, C.c_uint32),
                          P(tg, C.c_uint32), P(cm, C.c_uint64), P(mats, C.c_double), P(st.view(np.float64), C.c_double),
                          C.byref(ns))
     return st, ns.value
@@ -57,11 +58,14 @@ def oracle_apply(n, gates, psi):
     return o.cheat()[1]
 
 
+@pytest.mark.parametrize("r,rho", [(0, 4), (4, 4), (3, 3), (2, 3)])
 @pytest.mark.parametrize("n,L,m,seed", [(9, 6, 3, 0), (10, 7, 4, 1), (11, 8, 5, 2), (6, 6, 3, 3), (12, 12, 5, 4)])
-def test_planned_stages_equal_gate_by_gate(lib, n, L, m, seed):
+def test_planned_stages_equal_gate_by_gate(lib, n, L, m, seed, r, rho):
+    """r = 0 executes the per-operation stage kernel's semantics, r > 0 the
+    register-substage kernel's (swizzled tile, 2^r amplitudes per row)."""
     gates = random_mixed_circuit(n, 120, seed, kmax=3, max_ctrl=3)
     psi = random_state(n, seed=seed)
-    got, nst = plan_apply(lib, n, L, m, gates, psi)
+    got, nst = plan_apply(lib, n, L, m, gates, psi, r, rho)
     exp = oracle_apply(n, gates, psi)
     assert np.max(np.abs(got - exp)) < 1e-12
     assert nst >= 1
@@ -71,7 +75,7 @@ def test_random_circuit_packs_many_gates_per_stage(lib):
     n = 14
     gates = config2_circuit(n, depth=10, per_layer=14, seed=3)
     psi = random_state(n, seed=3)
-    got, nst = plan_apply(lib, n, 11, 5, gates, psi)
+    got, nst = plan_apply(lib, n, 12, 5, gates, psi, r=4, rho=4)
     exp = oracle_apply(n, gates, psi)
     assert np.max(np.abs(got - exp)) < 1e-12
     assert len(gates) / nst >= 8  # gates per pass over the state
