@@ -998,7 +998,7 @@ void Engine::run_staged() {
       bytes += stage_subs_bytes(sp) + (sp.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16;
     else
       bytes += (sp.ops.size() * sizeof(StageOpDev) + 15) / 16 * 16;
-    off_pool[i] = bytes;
+    off_pool[i] = bytes;  // for register stages the pool directly follows the operations
     bytes += (sp.pool.size() * esz + 15) / 16 * 16;
   }
   char *dev = nullptr;

@@ -279,14 +279,19 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
 
 template <typename T, int R>
 __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
-                                                        const SubstageDev *__restrict__ subs, int nsubs,
-                                                        const SubOpDev *__restrict__ ops,
-                                                        const cplx_t<T> *__restrict__ pool, uint32_t rho) {
+                                                        const unsigned char *__restrict__ table, uint32_t nsubs,
+                                                        uint32_t sops_off, uint32_t pool_off, uint32_t table_bytes,
+                                                        uint32_t rho) {
+  // Shared memory: the tile (2^L amplitudes, swizzled), the segment offsets,
+  // then a copy of the stage's table (substages, operations, matrices) so the
+  // per-operation reads are shared-memory broadcasts.
   using C = cplx_t<T>;
+  constexpr uint32_t TS = 1u << (R + 8);
+  constexpr int PER = sizeof(T) == 4 ? TS / 512 : TS / 256;  // 16-byte loads per thread per tile
   extern __shared__ __align__(16) unsigned char smem[];
-  const uint32_t TS = 1u << A.L;
   C *tile = reinterpret_cast<C *>(smem);
   uint64_t *segoff = reinterpret_cast<uint64_t *>(smem + size_t(TS) * sizeof(C));
+  unsigned char *tab = smem + size_t(TS) * sizeof(C) + (size_t(1) << A.h) * 8;
   const uint32_t nseg = 1u << A.h;
   for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
     uint64_t o = 0;
@@ -294,24 +299,42 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
       if ((s >> b) & 1) o |= uint64_t(1) << A.lpos[A.m + b];
     segoff[s] = o;
   }
+  for (uint32_t i = threadIdx.x; i < table_bytes / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(tab)[i] = reinterpret_cast<const uint4 *>(table)[i];
   __syncthreads();
+  const SubstageDev *subs = reinterpret_cast<const SubstageDev *>(tab);
+  const SubOpDev *ops = reinterpret_cast<const SubOpDev *>(tab + sops_off);
+  const C *pool = reinterpret_cast<const C *>(tab + pool_off);
   const uint32_t row = threadIdx.x;
   const uint32_t mask = (1u << A.m) - 1;
   for (uint64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
     const uint64_t base = insert_zeros(t, A.lpos, int(A.L));
+    // Issue every load of the tile before the first shared-memory store.
     if constexpr (sizeof(T) == 4) {
-      for (uint32_t v2 = threadIdx.x; v2 < (TS >> 1); v2 += blockDim.x) {
-        const uint32_t p = v2 << 1;
-        const float4 x = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p >> A.m] + (p & mask)));
-        tile[swz(p, rho)] = make_float2(x.x, x.y);
-        tile[swz(p + 1, rho)] = make_float2(x.z, x.w);
+      float4 x[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t p = (threadIdx.x + i * 256u) << 1;
+        x[i] = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p >> A.m] + (p & mask)));
+      }
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t p = (threadIdx.x + i * 256u) << 1;
+        tile[swz(p, rho)] = make_float2(x[i].x, x[i].y);
+        tile[swz(p + 1, rho)] = make_float2(x[i].z, x[i].w);
       }
     } else {
-      for (uint32_t p = threadIdx.x; p < TS; p += blockDim.x)
-        tile[swz(p, rho)] = __ldcs(psi + base + segoff[p >> A.m] + (p & mask));
+      C x[PER];
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t p = threadIdx.x + i * 256u;
+        x[i] = __ldcs(psi + base + segoff[p >> A.m] + (p & mask));
+      }
+#pragma unroll
+      for (int i = 0; i < PER; ++i) tile[swz(threadIdx.x + i * 256u, rho)] = x[i];
     }
     __syncthreads();
-    for (int si = 0; si < nsubs; ++si) {
+    for (uint32_t si = 0; si < nsubs; ++si) {
       const SubstageDev &S = subs[si];
       uint32_t srow = 0;
 #pragma unroll
@@ -320,8 +343,9 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
       C v[1 << R];
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j) v[j] = tile[srow ^ S.soff[j]];
-      for (uint32_t o = S.op_begin; o < S.op_end; ++o) {
-        const SubOpDev op = ops[o];
+      const uint32_t o1 = S.op_end;
+      for (uint32_t o = S.op_begin; o < o1; ++o) {
+        const SubOpDev &op = ops[o];
         if ((base & op.gctrl) != op.gctrl) continue;
         if ((row & op.tctrl) != op.tctrl) continue;
         reg_apply<T, R>(v, op, pool + op.mat, row, base);
@@ -331,14 +355,18 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
       __syncthreads();
     }
     if constexpr (sizeof(T) == 4) {
-      for (uint32_t v2 = threadIdx.x; v2 < (TS >> 1); v2 += blockDim.x) {
-        const uint32_t p = v2 << 1;
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t p = (threadIdx.x + i * 256u) << 1;
         const float2 a = tile[swz(p, rho)], b = tile[swz(p + 1, rho)];
         __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & mask)), make_float4(a.x, a.y, b.x, b.y));
       }
     } else {
-      for (uint32_t p = threadIdx.x; p < TS; p += blockDim.x)
+#pragma unroll
+      for (int i = 0; i < PER; ++i) {
+        const uint32_t p = threadIdx.x + i * 256u;
         __stcs(psi + base + segoff[p >> A.m] + (p & mask), tile[swz(p, rho)]);
+      }
     }
     __syncthreads();
   }
@@ -375,24 +403,27 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
     attr_set = true;
   }
   if (!plan.subs.empty()) {
-    // Register substages: d_ops holds the SubstageDev array, then the SubOpDev array.
+    // Register substages: d_ops holds the table [SubstageDev...][SubOpDev...][pool].
     constexpr int R = sizeof(T) == 4 ? 4 : 3;
     if (plan.r != unsigned(R) || plan.L != unsigned(R) + 8) return cudaErrorInvalidValue;
+    const uint32_t sops_off = uint32_t(stage_subs_bytes(plan));
+    const uint32_t pool_off = sops_off + uint32_t((plan.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16);
+    const uint32_t table_bytes = pool_off + uint32_t((plan.pool.size() * sizeof(cplx_t<T>) + 15) / 16 * 16);
+    const size_t smem_reg = smem + table_bytes;
+    if (smem_reg > 200 * 1024) return cudaErrorInvalidValue;
     static bool reg_attr = false;
     if (!reg_attr) {
-      cudaFuncSetAttribute(stage_reg_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+      cudaFuncSetAttribute(stage_reg_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
       reg_attr = true;
     }
     int per_sm = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_reg_kernel<T, R>, 256, smem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_reg_kernel<T, R>, 256, smem_reg);
     per_sm = std::max(1, per_sm);
     const uint64_t grid = std::min<uint64_t>(A.ntiles, uint64_t(stage_sms()) * per_sm);
-    const auto *subs = static_cast<const SubstageDev *>(d_ops);
-    const auto *sops = reinterpret_cast<const SubOpDev *>(static_cast<const char *>(d_ops) +
-                                                          stage_subs_bytes(plan));
-    stage_reg_kernel<T, R><<<unsigned(grid), 256, smem, s>>>(static_cast<cplx_t<T> *>(psi), A, subs,
-                                                             int(plan.subs.size()), sops,
-                                                             static_cast<const cplx_t<T> *>(d_pool), plan.rho);
+    stage_reg_kernel<T, R><<<unsigned(grid), 256, smem_reg, s>>>(static_cast<cplx_t<T> *>(psi), A,
+                                                                 static_cast<const unsigned char *>(d_ops),
+                                                                 uint32_t(plan.subs.size()), sops_off, pool_off,
+                                                                 table_bytes, plan.rho);
     return cudaGetLastError();
   }
   int per_sm = 1;
