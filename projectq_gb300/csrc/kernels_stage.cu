@@ -207,6 +207,18 @@ __device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], const SubOpDe
   }
 }
 
+template <typename T, int R, int B>
+__device__ __forceinline__ void reg_swap(cplx_t<T> (&v)[1 << R], uint32_t jctrl) {
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) {
+    if ((j >> B) & 1) continue;
+    if ((uint32_t(j) & jctrl) != jctrl) continue;
+    const cplx_t<T> a = v[j];
+    v[j] = v[j | (1 << B)];
+    v[j | (1 << B)] = a;
+  }
+}
+
 template <typename T, int R, int B0, int B1>
 __device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
   cplx_t<T> mm[16];
@@ -237,22 +249,28 @@ template <typename T, int R>
 __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M,
                                           uint32_t row, uint64_t base) {
   if (op.kind == 2) {
+    // index bits from row and non-local qubits (once), register qubits (table)
     uint32_t cidx = 0;
-#pragma unroll
-    for (int q = 0; q < 6; ++q) {
-      if (q >= int(op.dk)) break;
+    for (int q = 0; q < int(op.dk); ++q) {
       if (op.dloc[q] == 1) cidx |= ((row >> op.didx[q]) & 1u) << q;
       else if (op.dloc[q] == 2) cidx |= uint32_t((base >> op.didx[q]) & 1) << q;
     }
+    const uint4 jt = *reinterpret_cast<const uint4 *>(op.jidx);
+    const uint32_t jw[4] = {jt.x, jt.y, jt.z, jt.w};
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
-      uint32_t idx = cidx;
-#pragma unroll
-      for (int q = 0; q < 6; ++q) {
-        if (q >= int(op.dk)) break;
-        if (op.dloc[q] == 0) idx |= ((uint32_t(j) >> op.didx[q]) & 1u) << q;
-      }
+      const uint32_t idx = cidx | ((jw[j >> 2] >> (8 * (j & 3))) & 0xFFu);
       v[j] = cmul<T>(v[j], M[idx]);
+    }
+    return;
+  }
+  if (op.kind == 0 && op.swap) {
+    // exactly X on a register bit (CNOT, Toffoli...): exchange registers
+    switch (op.rb[0]) {
+      case 0: reg_swap<T, R, 0>(v, op.jctrl); break;
+      case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op.jctrl); break;
+      case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op.jctrl); break;
+      case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op.jctrl); break;
     }
     return;
   }
@@ -291,7 +309,8 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
   extern __shared__ __align__(16) unsigned char smem[];
   C *tile = reinterpret_cast<C *>(smem);
   uint64_t *segoff = reinterpret_cast<uint64_t *>(smem + size_t(TS) * sizeof(C));
-  unsigned char *tab = smem + size_t(TS) * sizeof(C) + (size_t(1) << A.h) * 8;
+  // the table starts 16-byte aligned (the segment table can be a single entry)
+  unsigned char *tab = smem + size_t(TS) * sizeof(C) + (((size_t(1) << A.h) * 8 + 15) & ~size_t(15));
   const uint32_t nseg = 1u << A.h;
   for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
     uint64_t o = 0;
@@ -409,7 +428,8 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
     const uint32_t sops_off = uint32_t(stage_subs_bytes(plan));
     const uint32_t pool_off = sops_off + uint32_t((plan.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16);
     const uint32_t table_bytes = pool_off + uint32_t((plan.pool.size() * sizeof(cplx_t<T>) + 15) / 16 * 16);
-    const size_t smem_reg = smem + table_bytes;
+    const size_t smem_reg = (size_t(1) << A.L) * sizeof(cplx_t<T>) + (((size_t(1) << A.h) * 8 + 15) & ~size_t(15)) +
+                            table_bytes;
     if (smem_reg > 200 * 1024) return cudaErrorInvalidValue;
     static bool reg_attr = false;
     if (!reg_attr) {

@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <complex>
 #include <cstdint>
+#include <cstddef>
 #include <cstring>
 #include <vector>
 
@@ -62,19 +63,23 @@ struct StageOpDev {
 // swizzled order s(p) = p ^ fold(p >> rho), fold XOR-ing rho-bit chunks, so
 // tile bit b lands in bank class b mod rho; the five lane bits are chosen to
 // cover every class, which makes each register access conflict-free.
-struct SubOpDev {
+struct alignas(16) SubOpDev {
+  uint8_t jidx[16]; // diagonal: index bits contributed by the register qubits, per j (16-byte aligned)
+  uint64_t gctrl;   // non-local controls (global mask)
   uint32_t kind;    // 0 dense 1-qubit, 1 dense 2-qubit, 2 diagonal
   uint32_t mat;     // offset in the stage's pool
   uint32_t jctrl;   // controls among the register bits (mask over j)
   uint32_t tctrl;   // controls among the row bits (mask over the row index)
-  uint64_t gctrl;   // non-local controls (global mask)
   uint8_t rb[2];    // dense: register-bit index of matrix bit 0 / 1
   uint8_t ek[4];    // dense 1-qubit: kinds of m00 m01 m10 m11 (0 zero, 1 real, 2 imag, 3 complex)
   uint8_t dk;       // diagonal: number of qubits
   uint8_t dloc[6];  // diagonal qubit q: 0 register bit, 1 row bit, 2 non-local
   uint8_t didx[6];  //   its register-bit index / row-bit index / global bit position
-  uint8_t pad[3];
+  uint8_t swap;     // dense 1-qubit: 1 if the matrix is exactly [[0, 1], [1, 0]]
+  uint8_t pad[2];
 };
+static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
+static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with one 16-byte load");
 struct SubstageDev {
   uint32_t op_begin, op_end;
   uint32_t soff[16];   // swizzled offset of register index j (XOR with the row's offset)
@@ -190,6 +195,12 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
       if (op.kind == 1) {
         so.kind = 2;
         so.dk = uint8_t(op.k);
+        for (uint32_t x = 0; x < (1u << r) && x < 16; ++x) {
+          uint32_t idx = 0;
+          for (unsigned q = 0; q < op.k; ++q)
+            if (op.tbit[q] != 0xFF && ((R >> op.tbit[q]) & 1) && ((x >> reg_index(op.tbit[q])) & 1)) idx |= 1u << q;
+          so.jidx[x] = uint8_t(idx);
+        }
         for (unsigned q = 0; q < op.k; ++q) {
           if (op.tbit[q] == 0xFF) {
             so.dloc[q] = 2;
@@ -205,11 +216,15 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
       } else {
         so.kind = op.k == 1 ? 0 : 1;
         for (unsigned q = 0; q < op.k; ++q) so.rb[q] = uint8_t(reg_index(op.tbit[q]));
-        if (op.k == 1)
+        if (op.k == 1) {
           for (int e = 0; e < 4; ++e) {
             const cplx z = sp.pool[op.mat + e];
             so.ek[e] = uint8_t((z.real() != 0. ? 1 : 0) | (z.imag() != 0. ? 2 : 0));
           }
+          const cplx *mm = &sp.pool[op.mat];
+          so.swap = mm[0] == cplx(0., 0.) && mm[1] == cplx(1., 0.) && mm[2] == cplx(1., 0.) &&
+                    mm[3] == cplx(0., 0.);
+        }
       }
       sp.sops.push_back(so);
     }
