@@ -55,6 +55,7 @@ extern "C" {
 #define GSIM_FUSION_REFERENCE 0 /* simulator.hpp:204-222 + fusion.hpp, window 4..5 */
 #define GSIM_FUSION_NONE 1      /* every gate is its own pass */
 #define GSIM_FUSION_STAGED 2    /* shared-memory tiles: many gates per HBM pass */
+#define GSIM_FUSION_LEARNED 3   /* per flush, the planner a learned cost model predicts fastest */
 
 #if defined(__GNUC__)
 #define GSIM_API __attribute__((visibility("default")))
@@ -259,6 +260,30 @@ GSIM_API int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *k
                                    const uint8_t *op_pauli, const double *coeffs, size_t nterms,
                                    const uint32_t *ids, size_t nids, uint32_t checkpoint_every,
                                    double *energy, double *grad);
+
+/* ---- Learned fusion planner (no reference counterpart) ----------------------
+ * gsim_plan_features: the 16 cost-model features of executing the queued
+ * gates (staged / learned modes queue gates until run) with planner `mode`
+ * (GSIM_FUSION_STAGED, _REFERENCE or _NONE), from a dry run of that planner.
+ * gsim_set_cost_model: install trained weights (nfeatures = 16, `hidden`
+ * units per layer, layout of gsim_mlp_get_params) for GSIM_FUSION_LEARNED.
+ * gsim_last_plan_choice: the planner the last learned flush used. */
+GSIM_API int gsim_plan_features(gsim_engine *e, int mode, float *out, size_t n);
+GSIM_API int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *params);
+GSIM_API int gsim_last_plan_choice(gsim_engine *e, int *mode);
+
+/* The cost model's network: F inputs -> H -> H -> 1 (ReLU), FP32, with
+ * hand-written forward, backward and Adam kernels (mlp.cu).  Parameters are
+ * one array: W1[H][F], b1[H], W2[H][H], b2[H], W3[H], b3. */
+GSIM_API int gsim_mlp_create(int F, int H, uint32_t seed, void **out);
+GSIM_API int gsim_mlp_destroy(void *mlp);
+GSIM_API int gsim_mlp_num_params(void *mlp, size_t *out);
+GSIM_API int gsim_mlp_get_params(void *mlp, float *out);
+GSIM_API int gsim_mlp_set_params(void *mlp, const float *in);
+GSIM_API int gsim_mlp_predict(void *mlp, const float *X, int B, float *out);
+GSIM_API int gsim_mlp_gradient(void *mlp, const float *X, const float *y, int B, float *grad, double *loss);
+GSIM_API int gsim_mlp_train(void *mlp, const float *X, const float *y, int B, int epochs, float lr,
+                            double *loss);
 
 /* ---- Allocation-free probability (no counterpart in the reference) ----------
  * Sum of |psi_i|^2 over the indices i with (i & mask) == value, for a state

@@ -27,6 +27,7 @@ GSIM_C64 = 1
 GSIM_FUSION_REFERENCE = 0
 GSIM_FUSION_NONE = 1
 GSIM_FUSION_STAGED = 2
+GSIM_FUSION_LEARNED = 3
 
 _u32p = C.POINTER(C.c_uint32)
 _u8p = C.POINTER(C.c_uint8)
@@ -115,6 +116,19 @@ PRODUCT_ONLY = {
         [_eng, _sz, _u8p, _u32p, _u32p, _u32p, C.POINTER(C.c_int32), _f64p, _f64p, _sz, _u32p, _u32p, _u8p,
          _f64p, _sz, _u32p, _sz, C.c_uint32, _f64p, _f64p],
     ),
+    "plan_features": (C.c_int, [_eng, C.c_int, C.POINTER(C.c_float), _sz]),
+    "set_cost_model": (C.c_int, [_eng, C.c_int, C.c_int, C.POINTER(C.c_float)]),
+    "last_plan_choice": (C.c_int, [_eng, C.POINTER(C.c_int)]),
+    "mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "mlp_destroy": (C.c_int, [C.c_void_p]),
+    "mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(_sz)]),
+    "mlp_get_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "mlp_set_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_float)]),
+    "mlp_predict": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_float)]),
+    "mlp_gradient": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int,
+                               C.POINTER(C.c_float), C.POINTER(C.c_double)]),
+    "mlp_train": (C.c_int, [C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_float), C.c_int, C.c_int, C.c_float,
+                            C.POINTER(C.c_double)]),
     "probability_noalloc": (
         C.c_int,
         [C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_uint64, _f64p, C.c_void_p],

@@ -222,7 +222,7 @@ class Engine {
         fail(GSIM_ERR_VALUE, "apply_controlled_gate(): a control is also a target or repeated");
     }
     counters_[0] += 1;
-    if (mode_ == GSIM_FUSION_STAGED) {
+    if (mode_ == GSIM_FUSION_STAGED || mode_ == GSIM_FUSION_LEARNED) {
       queue_.push_back(QueuedGate{std::move(m), ids, ctrl});
       if (queue_.size() >= kMaxQueue) run();
       return;
@@ -250,6 +250,10 @@ class Engine {
   void run() {
     if (mode_ == GSIM_FUSION_STAGED) {
       run_staged();
+      return;
+    }
+    if (mode_ == GSIM_FUSION_LEARNED) {
+      run_learned();
       return;
     }
     if (fused_.size() < 1) return;
@@ -599,10 +603,29 @@ class Engine {
     CK(cudaStreamSynchronize(stream_));
   }
 
+  // ---- learned planner -----------------------------------------------------
+  // Features of executing the queued gates with planner `mode` (dry run):
+  // the cost model's input.  Only meaningful in the staged / learned modes,
+  // where gates are queued until run().
+  static constexpr int kFeatures = 16;
+  void plan_features(int mode, float *f) {
+    std::vector<StageGate> gates = queued_positions();
+    plan_features_of(gates, mode, f);
+  }
+  void set_cost_model(int F, int H, const float *params) {
+    if (F != kFeatures || H < 1 || H > 256) fail(GSIM_ERR_VALUE, "cost model: unexpected layer sizes");
+    cm_H_ = H;
+    cm_.assign(params, params + (size_t(H) * F + H + size_t(H) * H + H + H + 1));
+  }
+  int last_choice() const { return last_choice_; }
+
   void set_fusion(int mode, unsigned kmax) {
     run();
-    if (mode != GSIM_FUSION_REFERENCE && mode != GSIM_FUSION_NONE && mode != GSIM_FUSION_STAGED)
+    if (mode != GSIM_FUSION_REFERENCE && mode != GSIM_FUSION_NONE && mode != GSIM_FUSION_STAGED &&
+        mode != GSIM_FUSION_LEARNED)
       fail(GSIM_ERR_VALUE, "unknown fusion mode");
+    if (mode == GSIM_FUSION_LEARNED && cm_.empty())
+      fail(GSIM_ERR_VALUE, "the learned planner needs a cost model (gsim_set_cost_model)");
     mode_ = mode;
     if (kmax) kmax_ = std::min(kmax, 5u);
     if (mode == GSIM_FUSION_STAGED && kmax >= 6) {  // kmax >= 6 selects the tile width in staged mode
@@ -754,6 +777,11 @@ class Engine {
 
   void run_staged();
   void exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool);
+  void run_learned();
+  std::vector<StageGate> queued_positions() const;
+  std::vector<DenseOp> reference_plan(const std::vector<StageGate> &gates) const;
+  void plan_features_of(const std::vector<StageGate> &gates, int mode, float *f) const;
+  float predict(const float *f) const;
 
   double masked_norm_host(uint64_t mask, uint64_t val) {
     double *d_norm = static_cast<double *>(small_.get(4096));
@@ -842,6 +870,9 @@ class Engine {
   std::vector<QueuedGate> queue_;
   unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
   bool use_reg_stages_ = true;
+  std::vector<float> cm_;  // cost-model weights (host copy)
+  int cm_H_ = 0;
+  int last_choice_ = -1;
   DevBuf upload_dev_;
   HostBuf upload_host_;
   cudaEvent_t upload_ev_ = nullptr;
@@ -1063,6 +1094,174 @@ void Engine::exec_stage(const StagePlan &sp, const void *d_ops, const void *d_po
   counters_[3] += 1;
 }
 
+
+std::vector<StageGate> Engine::queued_positions() const {
+  std::vector<StageGate> gates;
+  gates.reserve(queue_.size());
+  for (auto const &g : queue_) {
+    StageGate sg;
+    sg.m = g.m;
+    for (unsigned id : g.ids) sg.pos.push_back(pos_of(id));
+    for (unsigned c : g.ctrl) sg.ctrl_mask |= uint64_t(1) << pos_of(c);
+    gates.push_back(std::move(sg));
+  }
+  return gates;
+}
+
+// The reference's greedy fusion (simulator.hpp:204-222) replayed over a gate
+// list: the dense operations it would launch.
+std::vector<DenseOp> Engine::reference_plan(const std::vector<StageGate> &gates) const {
+  std::vector<DenseOp> out;
+  RefFusion cur;
+  auto flush = [&](RefFusion &f) {
+    if (f.size() < 1) return;
+    std::vector<cplx> M;
+    std::vector<unsigned> q, c;
+    f.compose(M, q, c);
+    DenseOp op;
+    op.m = std::move(M);
+    op.pos = q;  // positions were used as ids
+    for (unsigned x : c) op.ctrl_mask |= uint64_t(1) << x;
+    out.push_back(std::move(op));
+    f = RefFusion();
+  };
+  for (auto const &g : gates) {
+    std::vector<unsigned> ctrl;
+    for (unsigned b = 0; b < 64; ++b)
+      if ((g.ctrl_mask >> b) & 1) ctrl.push_back(b);
+    RefFusion f = cur;
+    f.insert(g.m, g.pos, ctrl);
+    const unsigned nf = f.num_qubits();
+    if (nf >= fmin_ && nf <= fmax_) {
+      cur = std::move(f);
+      flush(cur);
+    } else if (nf > fmax_ || (nf - unsigned(g.pos.size())) > cur.num_qubits()) {
+      flush(cur);
+      cur.insert(g.m, g.pos, ctrl);
+    } else {
+      cur = std::move(f);
+    }
+  }
+  flush(cur);
+  return out;
+}
+
+// 16 features: state size, precision, gate count, the candidate planner and
+// the launches, bytes and arithmetic of its plan (all log-scaled).
+void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, float *f) const {
+  std::fill(f, f + kFeatures, 0.f);
+  const double B = double(bpa_);
+  double launches = 0, bytes = 0, flops = 0, ops = 0, subs = 0, wide = 0;
+  auto dense_cost = [&](const DenseOp &op) {
+    const unsigned c = unsigned(__builtin_popcountll(op.ctrl_mask));
+    const double touched = std::ldexp(1.0, int(N_) - int(c));
+    launches += 1;
+    bytes += 2 * touched * B;
+    flops += touched * double(size_t(1) << op.pos.size());
+    if (op.pos.size() >= 3) wide += 1;
+  };
+  if (mode == GSIM_FUSION_STAGED) {
+    const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
+    StagePlanner planner(N_, L, prec_ == GSIM_C64 ? 5 : 4);
+    auto steps = planner.plan(gates);
+    const unsigned r = prec_ == GSIM_C64 ? 4 : 3, rho = r;
+    for (auto &st : steps) {
+      if (!st.is_stage) {
+        dense_cost(st.dense);
+        continue;
+      }
+      if (st.stage.L == r + 8) build_substages(st.stage, r, rho);
+      launches += 1;
+      bytes += 2 * std::ldexp(1.0, int(N_)) * B;
+      ops += double(st.stage.ops.size());
+      subs += double(st.stage.subs.size());
+      flops += std::ldexp(1.0, int(N_)) * double(st.stage.ops.size());
+    }
+  } else if (mode == GSIM_FUSION_REFERENCE) {
+    for (auto const &op : reference_plan(gates)) dense_cost(op);
+  } else {
+    for (auto const &g : gates) {
+      DenseOp op;
+      op.pos = g.pos;
+      op.ctrl_mask = g.ctrl_mask;
+      dense_cost(op);
+    }
+  }
+  auto lg = [](double x) { return float(std::log2(1.0 + x)); };
+  f[0] = float(N_) / 32.f;
+  f[1] = prec_ == GSIM_C64 ? 1.f : 0.f;
+  f[2] = lg(double(gates.size())) / 16.f;
+  f[3] = mode == GSIM_FUSION_STAGED ? 1.f : 0.f;
+  f[4] = mode == GSIM_FUSION_REFERENCE ? 1.f : 0.f;
+  f[5] = mode == GSIM_FUSION_NONE ? 1.f : 0.f;
+  f[6] = lg(launches) / 16.f;
+  f[7] = lg(bytes) / 48.f;
+  f[8] = lg(flops) / 48.f;
+  f[9] = lg(ops) / 16.f;
+  f[10] = lg(subs) / 16.f;
+  f[11] = lg(wide) / 16.f;
+  f[12] = float(std::ldexp(1.0, int(N_)) * B <= 96e6);  // state fits in L2
+  f[13] = lg(bytes / std::max(1.0, launches)) / 48.f;
+  f[14] = float(launches / std::max<double>(1.0, double(gates.size())));
+  f[15] = 1.f;
+}
+
+float Engine::predict(const float *x) const {
+  const int F = kFeatures, H = cm_H_;
+  const float *W1 = cm_.data(), *b1 = W1 + size_t(H) * F, *W2 = b1 + H, *b2 = W2 + size_t(H) * H, *W3 = b2 + H,
+              *b3 = W3 + H;
+  std::vector<float> a1(H), a2(H);
+  for (int o = 0; o < H; ++o) {
+    float s = b1[o];
+    for (int i = 0; i < F; ++i) s = std::fma(W1[o * F + i], x[i], s);
+    a1[o] = std::max(s, 0.f);
+  }
+  for (int o = 0; o < H; ++o) {
+    float s = b2[o];
+    for (int i = 0; i < H; ++i) s = std::fma(W2[o * H + i], a1[i], s);
+    a2[o] = std::max(s, 0.f);
+  }
+  float s = b3[0];
+  for (int i = 0; i < H; ++i) s = std::fma(W3[i], a2[i], s);
+  return s;
+}
+
+// GSIM_FUSION_LEARNED: predict the run time of the queued gates under each
+// planner and execute the cheapest plan.
+void Engine::run_learned() {
+  if (queue_.empty()) return;
+  std::vector<StageGate> gates = queued_positions();
+  int best = GSIM_FUSION_STAGED;
+  float best_t = 0.f;
+  bool first = true;
+  for (int mode : {GSIM_FUSION_STAGED, GSIM_FUSION_REFERENCE, GSIM_FUSION_NONE}) {
+    float f[kFeatures];
+    plan_features_of(gates, mode, f);
+    const float t = predict(f);
+    if (first || t < best_t) {
+      best = mode;
+      best_t = t;
+      first = false;
+    }
+  }
+  last_choice_ = best;
+  if (best == GSIM_FUSION_STAGED) {
+    run_staged();
+    return;
+  }
+  queue_.clear();
+  if (best == GSIM_FUSION_REFERENCE) {
+    for (auto const &op : reference_plan(gates)) exec_dense(op);
+  } else {
+    for (auto &g : gates) {
+      DenseOp op;
+      op.m = std::move(g.m);
+      op.pos = g.pos;
+      op.ctrl_mask = g.ctrl_mask;
+      exec_dense(op);
+    }
+  }
+}
 }  // namespace gsim
 
 // ===========================================================================
@@ -1426,6 +1625,18 @@ int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *kind, cons
 }
 int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out) {
   return guard([&] { E(a)->compare(*E(b), out); });
+}
+int gsim_plan_features(gsim_engine *e, int mode, float *out, size_t n) {
+  return guard([&] {
+    if (n < size_t(Engine::kFeatures)) fail(GSIM_ERR_LENGTH, "plan_features(): output too small");
+    E(e)->plan_features(mode, out);
+  });
+}
+int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *params) {
+  return guard([&] { E(e)->set_cost_model(nfeatures, hidden, params); });
+}
+int gsim_last_plan_choice(gsim_engine *e, int *mode) {
+  return guard([&] { *mode = E(e)->last_choice(); });
 }
 int gsim_set_device(int device) {
   return guard([&] { CK(cudaSetDevice(device)); });

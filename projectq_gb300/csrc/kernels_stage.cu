@@ -188,31 +188,60 @@ __device__ __forceinline__ void cmac_k(int kd, cplx_t<T> m, cplx_t<T> v, T &re, 
   }
 }
 
-template <typename T, int R, int B>
-__device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+// One 1-qubit operation on register bit B, matrix class CLS (stage.hpp):
+// 0 general complex, 1 real, 2 real diagonal / imaginary off-diagonal,
+// 4 anti-diagonal.  `amask` selects the group bases j the operation touches.
+template <typename T, int R, int B, int CLS>
+__device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], uint32_t amask, const cplx_t<T> *M) {
   const cplx_t<T> m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
-  const int k0 = op.ek[0], k1 = op.ek[1], k2 = op.ek[2], k3 = op.ek[3];
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if ((j >> B) & 1) continue;
-    if ((uint32_t(j) & op.jctrl) != op.jctrl) continue;
+    if (!((amask >> j) & 1)) continue;
     const cplx_t<T> a = v[j], b = v[j | (1 << B)];
-    T r0 = T(0), i0 = T(0), r1 = T(0), i1 = T(0);
-    cmac_k<T>(k0, m00, a, r0, i0);
-    cmac_k<T>(k1, m01, b, r0, i0);
-    cmac_k<T>(k2, m10, a, r1, i1);
-    cmac_k<T>(k3, m11, b, r1, i1);
+    T r0, i0, r1, i1;
+    if constexpr (CLS == 1) {
+      r0 = fma(m00.x, a.x, m01.x * b.x);
+      i0 = fma(m00.x, a.y, m01.x * b.y);
+      r1 = fma(m10.x, a.x, m11.x * b.x);
+      i1 = fma(m10.x, a.y, m11.x * b.y);
+    } else if constexpr (CLS == 2) {
+      r0 = fma(m00.x, a.x, -m01.y * b.y);
+      i0 = fma(m00.x, a.y, m01.y * b.x);
+      r1 = fma(-m10.y, a.y, m11.x * b.x);
+      i1 = fma(m10.y, a.x, m11.x * b.y);
+    } else if constexpr (CLS == 4) {
+      r0 = fma(m01.x, b.x, -m01.y * b.y);
+      i0 = fma(m01.x, b.y, m01.y * b.x);
+      r1 = fma(m10.x, a.x, -m10.y * a.y);
+      i1 = fma(m10.x, a.y, m10.y * a.x);
+    } else {
+      r0 = fma(m00.x, a.x, fma(-m00.y, a.y, fma(m01.x, b.x, -m01.y * b.y)));
+      i0 = fma(m00.x, a.y, fma(m00.y, a.x, fma(m01.x, b.y, m01.y * b.x)));
+      r1 = fma(m10.x, a.x, fma(-m10.y, a.y, fma(m11.x, b.x, -m11.y * b.y)));
+      i1 = fma(m10.x, a.y, fma(m10.y, a.x, fma(m11.x, b.y, m11.y * b.x)));
+    }
     v[j] = mkc<T>(r0, i0);
     v[j | (1 << B)] = mkc<T>(r1, i1);
   }
 }
 
 template <typename T, int R, int B>
-__device__ __forceinline__ void reg_swap(cplx_t<T> (&v)[1 << R], uint32_t jctrl) {
+__device__ __forceinline__ void reg_dense1_cls(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+  switch (op.cls) {
+    case 1: reg_dense1<T, R, B, 1>(v, op.amask, M); break;
+    case 2: reg_dense1<T, R, B, 2>(v, op.amask, M); break;
+    case 4: reg_dense1<T, R, B, 4>(v, op.amask, M); break;
+    default: reg_dense1<T, R, B, 0>(v, op.amask, M); break;
+  }
+}
+
+template <typename T, int R, int B>
+__device__ __forceinline__ void reg_swap(cplx_t<T> (&v)[1 << R], uint32_t amask) {
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if ((j >> B) & 1) continue;
-    if ((uint32_t(j) & jctrl) != jctrl) continue;
+    if (!((amask >> j) & 1)) continue;
     const cplx_t<T> a = v[j];
     v[j] = v[j | (1 << B)];
     v[j | (1 << B)] = a;
@@ -227,7 +256,7 @@ __device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDe
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if (((j >> B0) & 1) || ((j >> B1) & 1)) continue;
-    if ((uint32_t(j) & op.jctrl) != op.jctrl) continue;
+    if (!((op.amask >> j) & 1)) continue;
     const int j1 = j | (1 << B0), j2 = j | (1 << B1), j3 = j1 | (1 << B1);
     const cplx_t<T> x[4] = {v[j], v[j1], v[j2], v[j3]};
     cplx_t<T> y[4];
@@ -267,19 +296,19 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
   if (op.kind == 0 && op.swap) {
     // exactly X on a register bit (CNOT, Toffoli...): exchange registers
     switch (op.rb[0]) {
-      case 0: reg_swap<T, R, 0>(v, op.jctrl); break;
-      case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op.jctrl); break;
-      case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op.jctrl); break;
-      case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op.jctrl); break;
+      case 0: reg_swap<T, R, 0>(v, op.amask); break;
+      case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op.amask); break;
+      case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op.amask); break;
+      case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op.amask); break;
     }
     return;
   }
   if (op.kind == 0) {
     switch (op.rb[0]) {
-      case 0: reg_dense1<T, R, 0>(v, op, M); break;
-      case 1: if constexpr (R > 1) reg_dense1<T, R, 1>(v, op, M); break;
-      case 2: if constexpr (R > 2) reg_dense1<T, R, 2>(v, op, M); break;
-      case 3: if constexpr (R > 3) reg_dense1<T, R, 3>(v, op, M); break;
+      case 0: reg_dense1_cls<T, R, 0>(v, op, M); break;
+      case 1: if constexpr (R > 1) reg_dense1_cls<T, R, 1>(v, op, M); break;
+      case 2: if constexpr (R > 2) reg_dense1_cls<T, R, 2>(v, op, M); break;
+      case 3: if constexpr (R > 3) reg_dense1_cls<T, R, 3>(v, op, M); break;
     }
     return;
   }

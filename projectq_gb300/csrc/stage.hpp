@@ -76,7 +76,11 @@ struct alignas(16) SubOpDev {
   uint8_t dloc[6];  // diagonal qubit q: 0 register bit, 1 row bit, 2 non-local
   uint8_t didx[6];  //   its register-bit index / row-bit index / global bit position
   uint8_t swap;     // dense 1-qubit: 1 if the matrix is exactly [[0, 1], [1, 0]]
-  uint8_t pad[2];
+  uint8_t cls;      // dense 1-qubit matrix class: 0 general, 1 real, 2 real diagonal with
+                    // imaginary off-diagonal (Rx), 3 exact swap, 4 anti-diagonal
+  uint8_t pad;
+  uint32_t amask;   // dense: register indices j that are group bases with the controls satisfied
+  uint32_t pad2[3];
 };
 static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
 static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with one 16-byte load");
@@ -224,7 +228,15 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
           const cplx *mm = &sp.pool[op.mat];
           so.swap = mm[0] == cplx(0., 0.) && mm[1] == cplx(1., 0.) && mm[2] == cplx(1., 0.) &&
                     mm[3] == cplx(0., 0.);
+          const bool real = mm[0].imag() == 0. && mm[1].imag() == 0. && mm[2].imag() == 0. && mm[3].imag() == 0.;
+          const bool rx = mm[0].imag() == 0. && mm[3].imag() == 0. && mm[1].real() == 0. && mm[2].real() == 0.;
+          const bool anti = mm[0] == cplx(0., 0.) && mm[3] == cplx(0., 0.);
+          so.cls = so.swap ? 3 : real ? 1 : rx ? 2 : anti ? 4 : 0;
         }
+        uint32_t tm = 0;
+        for (unsigned q = 0; q < op.k; ++q) tm |= 1u << so.rb[q];
+        for (uint32_t x = 0; x < (1u << r); ++x)
+          if (!(x & tm) && (x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
       }
       sp.sops.push_back(so);
     }

@@ -29,7 +29,7 @@ from . import _lib
 _PRECISIONS = {"c128": _lib.GSIM_C128, "complex128": _lib.GSIM_C128, "c64": _lib.GSIM_C64,
                "complex64": _lib.GSIM_C64}
 _FUSION = {"reference": _lib.GSIM_FUSION_REFERENCE, "none": _lib.GSIM_FUSION_NONE,
-           "staged": _lib.GSIM_FUSION_STAGED}
+           "staged": _lib.GSIM_FUSION_STAGED, "learned": _lib.GSIM_FUSION_LEARNED}
 
 
 _PENDING = []

@@ -121,12 +121,40 @@ void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::Stag
               }
               v[j] *= M[idx];
             }
+          } else if (op.kind == 0) {
+            // the kernel's 1-qubit paths: group bases from amask, one formula per class
+            const unsigned B = op.rb[0];
+            const cplx m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
+            for (uint32_t j = 0; j < v.size(); ++j) {
+              if ((j >> B) & 1) continue;
+              if (!((op.amask >> j) & 1)) continue;
+              const cplx a = v[j], b = v[j | (1u << B)];
+              cplx o0, o1;
+              if (op.cls == 3) {
+                o0 = b;
+                o1 = a;
+              } else if (op.cls == 1) {
+                o0 = cplx(m00.real() * a.real() + m01.real() * b.real(), m00.real() * a.imag() + m01.real() * b.imag());
+                o1 = cplx(m10.real() * a.real() + m11.real() * b.real(), m10.real() * a.imag() + m11.real() * b.imag());
+              } else if (op.cls == 2) {
+                o0 = cplx(m00.real() * a.real() - m01.imag() * b.imag(), m00.real() * a.imag() + m01.imag() * b.real());
+                o1 = cplx(-m10.imag() * a.imag() + m11.real() * b.real(), m10.imag() * a.real() + m11.real() * b.imag());
+              } else if (op.cls == 4) {
+                o0 = m01 * b;
+                o1 = m10 * a;
+              } else {
+                o0 = m00 * a + m01 * b;
+                o1 = m10 * a + m11 * b;
+              }
+              v[j] = o0;
+              v[j | (1u << B)] = o1;
+            }
           } else {
             const unsigned k = op.kind == 0 ? 1 : 2, d = 1u << k;
             uint32_t tm = 0;
             for (unsigned q = 0; q < k; ++q) tm |= 1u << op.rb[q];
             for (uint32_t j = 0; j < v.size(); ++j) {
-              if ((j & tm) || (j & op.jctrl) != op.jctrl) continue;
+              if ((j & tm) || !((op.amask >> j) & 1)) continue;
               std::vector<uint32_t> jj(d);
               for (uint32_t a = 0; a < d; ++a) {
                 jj[a] = j;
