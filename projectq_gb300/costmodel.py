@@ -141,7 +141,7 @@ def features_for(n, gates, precision="c64"):
     return feats
 
 
-def time_plan(n, gates, fusion, precision="c64", repeats=2, cost_model=None):
+def time_plan(n, gates, fusion, precision="c64", repeats=1, cost_model=None):
     """Device milliseconds to apply `gates` with the given planner (engine
     CUDA events around submission and flush; the best of `repeats`)."""
     sim = Simulator(1, precision=precision, fusion="staged")
