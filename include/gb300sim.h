@@ -192,6 +192,10 @@ GSIM_API int gsim_synchronize(gsim_engine *e);
 /* Select the fusion planner (GSIM_FUSION_*) and its widest fused gate. */
 GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
 
+/* Use (on != 0, the default) or avoid the tcgen05 tensor-core kernel for
+ * fused complex64 gates of 5 or 6 targets (3xTF32 split precision). */
+GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int on);
+
 /* Preallocate device memory for nqubits qubits (avoids regrowth). */
 GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
 

@@ -24,7 +24,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = BUILD / "libgb300sim.so"
 
-SOURCES = ["engine.cu", "kernels_gate.cu", "kernels_state.cu", "kernels_stage.cu", "kernels_adjoint.cu", "mlp.cu", "noalloc.cu"]
+SOURCES = ["engine.cu", "kernels_gate.cu", "kernels_state.cu", "kernels_stage.cu", "kernels_adjoint.cu", "kernels_tc.cu", "mlp.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = [
     "-O3",

@@ -115,6 +115,9 @@ class Engine {
     pinned_.release();
     upload_host_.release();
     if (upload_ev_) cudaEventDestroy(upload_ev_);
+    mat_dev_.release();
+    mat_host_.release();
+    if (mat_ev_) cudaEventDestroy(mat_ev_);
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -248,6 +251,19 @@ class Engine {
 
   // ---- simulator.hpp:487-527 ----------------------------------------------
   void run() {
+    run_planned();
+    if (tc_used_) {
+      // a tensor-core launch records a timeout in a device flag: check it here
+      int h = 0;
+      int *d_err = reinterpret_cast<int *>(static_cast<char *>(small_.get(4096)) + 2048);
+      CK(cudaMemcpyAsync(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      tc_used_ = false;
+      if (h) fail(GSIM_ERR_CUDA, "tensor-core gate kernel: the MMA completion wait timed out");
+    }
+  }
+
+  void run_planned() {
     if (mode_ == GSIM_FUSION_STAGED) {
       run_staged();
       return;
@@ -634,6 +650,10 @@ class Engine {
     }
   }
   void reserve(unsigned nq) { ensure_capacity(nq); }
+  void set_tensor_cores(bool on) {
+    run();
+    use_tc_ = on;
+  }
 
   // ---- timing -------------------------------------------------------------
   void timer_mark(int slot) {
@@ -743,7 +763,32 @@ class Engine {
     const uint64_t bytes = 2 * (uint64_t(1) << (N_ - c)) * bpa_;
     int e0 = -1;
     if (profiling_) e0 = record_event();
-    CK(launch_dense(prec_, state_.p, N_, op, stream_));
+    const size_t kq = op.pos.size();
+    if (prec_ == GSIM_C64 && use_tc_ && (kq == 5 || kq == 6) && N_ >= kq + 7) {
+      // tensor cores: U embedded as a real 2^(k+1) square matrix, TF32 hi/lo
+      std::vector<float> hi, lo;
+      tc_split_unitary(op.m, int(kq), hi, lo);
+      if (mat_ev_) CK(cudaEventSynchronize(mat_ev_));
+      const size_t nb = hi.size() * 4;
+      char *h = static_cast<char *>(mat_host_.get(2 * nb));
+      std::memcpy(h, hi.data(), nb);
+      std::memcpy(h + nb, lo.data(), nb);
+      char *d = static_cast<char *>(mat_dev_.get(2 * nb));
+      CK(cudaMemcpyAsync(d, h, 2 * nb, cudaMemcpyHostToDevice, stream_));
+      if (!mat_ev_) CK(cudaEventCreateWithFlags(&mat_ev_, cudaEventDisableTiming));
+      CK(cudaEventRecord(mat_ev_, stream_));
+      int *d_err = reinterpret_cast<int *>(static_cast<char *>(small_.get(4096)) + 2048);
+      if (!tc_used_) CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
+      CK(launch_tc_gate(state_.p, N_, op, reinterpret_cast<const float *>(d),
+                        reinterpret_cast<const float *>(d + nb), d_err, stream_));
+      tc_used_ = true;
+    } else if (kq > 5) {
+      const size_t D = size_t(1) << op.pos.size();
+      void *dm = upload_matrix(op.m, D * D);
+      CK(launch_wide(prec_, state_.p, N_, op, dm, stream_));
+    } else {
+      CK(launch_dense(prec_, state_.p, N_, op, stream_));
+    }
     if (profiling_) {
       const int e1 = record_event();
       Prof p;
@@ -764,6 +809,27 @@ class Engine {
     counters_[2] += bytes;
     counters_[3] += 1;
   }
+  // Copy a matrix in the state's precision to device memory (a ring of
+  // buffers; the host staging buffer is reused only after its copy is done).
+  void *upload_matrix(const std::vector<cplx> &m, size_t count) {
+    const size_t bytes = count * bpa_;
+    if (mat_ev_) CK(cudaEventSynchronize(mat_ev_));
+    char *h = static_cast<char *>(mat_host_.get(bytes));
+    for (size_t i = 0; i < count; ++i) {
+      if (prec_ == GSIM_C64) {
+        reinterpret_cast<float *>(h)[2 * i] = float(m[i].real());
+        reinterpret_cast<float *>(h)[2 * i + 1] = float(m[i].imag());
+      } else {
+        reinterpret_cast<double *>(h)[2 * i] = m[i].real();
+        reinterpret_cast<double *>(h)[2 * i + 1] = m[i].imag();
+      }
+    }
+    void *d = mat_dev_.get(bytes);
+    CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, stream_));
+    if (!mat_ev_) CK(cudaEventCreateWithFlags(&mat_ev_, cudaEventDisableTiming));
+    CK(cudaEventRecord(mat_ev_, stream_));
+    return d;
+  }
   int record_event() {
     if (ev_next_ >= ev_pool_.size()) {
       cudaEvent_t ev;
@@ -776,11 +842,15 @@ class Engine {
   }
 
   void run_staged();
+  std::vector<PlanStep> plan_staged(const std::vector<StageGate> &gates) const;
+  void execute_staged(std::vector<PlanStep> &steps);
   void exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool);
   void run_learned();
+  void reference_counts(const std::vector<StageGate> &gates, std::vector<std::pair<unsigned, unsigned>> &launches) const;
   std::vector<StageGate> queued_positions() const;
   std::vector<DenseOp> reference_plan(const std::vector<StageGate> &gates) const;
-  void plan_features_of(const std::vector<StageGate> &gates, int mode, float *f) const;
+  void plan_features_of(const std::vector<StageGate> &gates, int mode, float *f,
+                        const std::vector<PlanStep> *staged = nullptr) const;
   float predict(const float *f) const;
 
   double masked_norm_host(uint64_t mask, uint64_t val) {
@@ -870,6 +940,11 @@ class Engine {
   std::vector<QueuedGate> queue_;
   unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
   bool use_reg_stages_ = true;
+  bool use_tc_ = true;
+  bool tc_used_ = false;
+  DevBuf mat_dev_;
+  HostBuf mat_host_;
+  cudaEvent_t mat_ev_ = nullptr;
   std::vector<float> cm_;  // cost-model weights (host copy)
   int cm_H_ = 0;
   int last_choice_ = -1;
@@ -994,19 +1069,7 @@ uint64_t Engine::sample(double rnd) {
   return pick - 1;
 }
 
-void Engine::run_staged() {
-  if (queue_.empty()) return;
-  std::vector<QueuedGate> q;
-  q.swap(queue_);
-  std::vector<StageGate> gates;
-  gates.reserve(q.size());
-  for (auto &g : q) {
-    StageGate sg;
-    sg.m = std::move(g.m);
-    for (unsigned id : g.ids) sg.pos.push_back(pos_of(id));
-    for (unsigned c : g.ctrl) sg.ctrl_mask |= uint64_t(1) << pos_of(c);
-    gates.push_back(std::move(sg));
-  }
+std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) const {
   // Tiles of 32 KB: 2^12 complex64 or 2^11 complex128 amplitudes, with runs
   // of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
   const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
@@ -1017,6 +1080,18 @@ void Engine::run_staged() {
   const unsigned r = prec_ == GSIM_C64 ? 4 : 3, rho = prec_ == GSIM_C64 ? 4 : 3;
   for (auto &st : steps)
     if (st.is_stage && use_reg_stages_ && st.stage.L == r + 8) build_substages(st.stage, r, rho);
+  return steps;
+}
+
+void Engine::run_staged() {
+  if (queue_.empty()) return;
+  std::vector<StageGate> gates = queued_positions();
+  queue_.clear();
+  std::vector<PlanStep> steps = plan_staged(gates);
+  execute_staged(steps);
+}
+
+void Engine::execute_staged(std::vector<PlanStep> &steps) {
   // Serialise every stage's operations and matrices into one upload.
   const size_t esz = bpa_;
   size_t bytes = 0;
@@ -1146,9 +1221,61 @@ std::vector<DenseOp> Engine::reference_plan(const std::vector<StageGate> &gates)
   return out;
 }
 
+// The reference's admission rule (simulator.hpp:204-222, fusion.hpp:130-160)
+// replayed on qubit sets only: (matrix qubits, shared controls) per launch.
+void Engine::reference_counts(const std::vector<StageGate> &gates,
+                              std::vector<std::pair<unsigned, unsigned>> &launches) const {
+  uint64_t qs = 0, cs = 0;
+  size_t items = 0;
+  auto flush = [&]() {
+    if (items) launches.emplace_back(unsigned(__builtin_popcountll(qs)), unsigned(__builtin_popcountll(cs)));
+    qs = cs = 0;
+    items = 0;
+  };
+  auto insert = [&](uint64_t &q, uint64_t &c, size_t &n, const StageGate &g) {
+    uint64_t t = 0;
+    for (unsigned p : g.pos) t |= uint64_t(1) << p;
+    q |= t;
+    uint64_t dropped = c & ~g.ctrl_mask;  // shared controls this gate lacks
+    const uint64_t fresh = g.ctrl_mask & ~c;
+    if (n) {
+      q |= fresh;  // new controls become matrix qubits
+    } else {
+      c |= fresh;
+    }
+    if (dropped) {
+      c &= ~dropped;
+      q |= dropped;
+    }
+    ++n;
+  };
+  for (auto const &g : gates) {
+    uint64_t q2 = qs, c2 = cs;
+    size_t n2 = items;
+    insert(q2, c2, n2, g);
+    const unsigned nf = unsigned(__builtin_popcountll(q2));
+    const unsigned nt = unsigned(g.pos.size());
+    if (nf >= fmin_ && nf <= fmax_) {
+      qs = q2;
+      cs = c2;
+      items = n2;
+      flush();
+    } else if (nf > fmax_ || (nf - nt) > unsigned(__builtin_popcountll(qs))) {
+      flush();
+      insert(qs, cs, items, g);
+    } else {
+      qs = q2;
+      cs = c2;
+      items = n2;
+    }
+  }
+  flush();
+}
+
 // 16 features: state size, precision, gate count, the candidate planner and
 // the launches, bytes and arithmetic of its plan (all log-scaled).
-void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, float *f) const {
+void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, float *f,
+                              const std::vector<PlanStep> *staged) const {
   std::fill(f, f + kFeatures, 0.f);
   const double B = double(bpa_);
   double launches = 0, bytes = 0, flops = 0, ops = 0, subs = 0, wide = 0;
@@ -1161,16 +1288,16 @@ void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, flo
     if (op.pos.size() >= 3) wide += 1;
   };
   if (mode == GSIM_FUSION_STAGED) {
-    const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
-    StagePlanner planner(N_, L, prec_ == GSIM_C64 ? 5 : 4);
-    auto steps = planner.plan(gates);
-    const unsigned r = prec_ == GSIM_C64 ? 4 : 3, rho = r;
-    for (auto &st : steps) {
+    std::vector<PlanStep> own;
+    if (!staged) {
+      own = plan_staged(gates);
+      staged = &own;
+    }
+    for (auto const &st : *staged) {
       if (!st.is_stage) {
         dense_cost(st.dense);
         continue;
       }
-      if (st.stage.L == r + 8) build_substages(st.stage, r, rho);
       launches += 1;
       bytes += 2 * std::ldexp(1.0, int(N_)) * B;
       ops += double(st.stage.ops.size());
@@ -1178,7 +1305,15 @@ void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, flo
       flops += std::ldexp(1.0, int(N_)) * double(st.stage.ops.size());
     }
   } else if (mode == GSIM_FUSION_REFERENCE) {
-    for (auto const &op : reference_plan(gates)) dense_cost(op);
+    std::vector<std::pair<unsigned, unsigned>> ls;  // (matrix qubits, controls) per launch
+    reference_counts(gates, ls);
+    for (auto const &l : ls) {
+      const double touched = std::ldexp(1.0, int(N_) - int(l.second));
+      launches += 1;
+      bytes += 2 * touched * B;
+      flops += touched * std::ldexp(1.0, int(l.first));
+      if (l.first >= 3) wide += 1;
+    }
   } else {
     for (auto const &g : gates) {
       DenseOp op;
@@ -1231,12 +1366,14 @@ float Engine::predict(const float *x) const {
 void Engine::run_learned() {
   if (queue_.empty()) return;
   std::vector<StageGate> gates = queued_positions();
+  queue_.clear();
+  std::vector<PlanStep> staged = plan_staged(gates);
   int best = GSIM_FUSION_STAGED;
   float best_t = 0.f;
   bool first = true;
   for (int mode : {GSIM_FUSION_STAGED, GSIM_FUSION_REFERENCE, GSIM_FUSION_NONE}) {
     float f[kFeatures];
-    plan_features_of(gates, mode, f);
+    plan_features_of(gates, mode, f, &staged);
     const float t = predict(f);
     if (first || t < best_t) {
       best = mode;
@@ -1246,11 +1383,8 @@ void Engine::run_learned() {
   }
   last_choice_ = best;
   if (best == GSIM_FUSION_STAGED) {
-    run_staged();
-    return;
-  }
-  queue_.clear();
-  if (best == GSIM_FUSION_REFERENCE) {
+    execute_staged(staged);
+  } else if (best == GSIM_FUSION_REFERENCE) {
     for (auto const &op : reference_plan(gates)) exec_dense(op);
   } else {
     for (auto &g : gates) {
@@ -1262,6 +1396,7 @@ void Engine::run_learned() {
     }
   }
 }
+
 }  // namespace gsim
 
 // ===========================================================================
@@ -1637,6 +1772,9 @@ int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *
 }
 int gsim_last_plan_choice(gsim_engine *e, int *mode) {
   return guard([&] { *mode = E(e)->last_choice(); });
+}
+int gsim_set_tensor_cores(gsim_engine *e, int on) {
+  return guard([&] { E(e)->set_tensor_cores(on != 0); });
 }
 int gsim_set_device(int device) {
   return guard([&] { CK(cudaSetDevice(device)); });

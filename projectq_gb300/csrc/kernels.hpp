@@ -14,6 +14,16 @@ namespace gsim {
 
 // prec: 0 = complex128 state, 1 = complex64 state.
 cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s);
+// Fused dense gates of 5 or 6 targets on a complex64 state with tcgen05
+// tensor cores (3xTF32).  d_bhi / d_blo: the real embedding of U split into
+// TF32 hi and lo parts (tc_split_unitary); *d_err is set on a timeout.
+void tc_split_unitary(const std::vector<cplx> &U, int k, std::vector<float> &hi, std::vector<float> &lo);
+cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_bhi, const float *d_blo,
+                           int *d_err, cudaStream_t s);
+// Gates of up to 7 targets; d_matrix: the 2^k x 2^k matrix (row-major) in the
+// state's precision in device memory.
+cudaError_t launch_wide(int prec, void *psi, unsigned nq, const DenseOp &op, const void *d_matrix,
+                        cudaStream_t s);
 
 // ---- stage kernel (many gates per pass through shared-memory tiles) -----
 struct StagePlan;  // defined in stage.hpp

@@ -106,6 +106,49 @@ __global__ void __launch_bounds__(256) dense_kernel_vec2(float2 *__restrict__ ps
   }
 }
 
+// Wide gates (k = 6, 7 targets, or any k): a CTA gathers whole amplitude
+// groups into shared memory, then each thread computes one output row of one
+// group, reading the matrix row from global memory (L1/L2 resident; 2^k x 2^k
+// complex).  Used for gates wider than the register kernels handle.
+struct WideArgs {
+  uint64_t units;      // number of groups
+  uint64_t ctrl_set;
+  int nins, k, gpb;    // insert count, targets, groups per block
+  uint8_t ins[64];
+  uint64_t off[128];   // offset of matrix index j
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) wide_kernel(cplx_t<T> *__restrict__ psi, const cplx_t<T> *__restrict__ U,
+                                                   const __grid_constant__ WideArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_w[];
+  cplx_t<T> *buf = reinterpret_cast<cplx_t<T> *>(smem_w);
+  const int D = 1 << A.k;
+  const int gl = threadIdx.x / D, r = threadIdx.x % D;  // local group, output row
+  for (uint64_t g0 = uint64_t(blockIdx.x) * A.gpb; g0 < A.units; g0 += uint64_t(gridDim.x) * A.gpb) {
+    const uint64_t g = g0 + gl;
+    const bool active = gl < A.gpb && g < A.units;
+    uint64_t base = 0;
+    if (active) {
+      base = insert_zeros(g, A.ins, A.nins) | A.ctrl_set;
+      buf[gl * D + r] = psi[base + A.off[r]];
+    }
+    __syncthreads();
+    if (active) {
+      T re = T(0), im = T(0);
+      const cplx_t<T> *row = U + size_t(r) * D;
+      const cplx_t<T> *v = buf + gl * D;
+      for (int j = 0; j < D; ++j) {
+        const cplx_t<T> m = __ldg(row + j), x = v[j];
+        re = fma(m.x, x.x, fma(-m.y, x.y, re));
+        im = fma(m.x, x.y, fma(m.y, x.x, im));
+      }
+      psi[base + A.off[r]] = mkc<T>(re, im);
+    }
+    __syncthreads();
+  }
+}
+
 namespace {
 
 int g_num_sms = 0;
@@ -185,6 +228,32 @@ cudaError_t launch_dense_k(T *, void *psi, unsigned nq, const DenseOp &op, cudaS
 }
 
 template <typename T>
+cudaError_t launch_wide_t(void *psi, unsigned nq, const DenseOp &op, const void *d_matrix, cudaStream_t s) {
+  WideArgs A;
+  std::memset(&A, 0, sizeof(A));
+  const int k = int(op.pos.size()), D = 1 << k;
+  std::vector<unsigned> ins(op.pos.begin(), op.pos.end());
+  for (unsigned b = 0; b < 64; ++b)
+    if ((op.ctrl_mask >> b) & 1) ins.push_back(b);
+  std::sort(ins.begin(), ins.end());
+  if (ins.size() > nq) throw std::invalid_argument("gate wider than the state");
+  A.nins = int(ins.size());
+  for (size_t i = 0; i < ins.size(); ++i) A.ins[i] = uint8_t(ins[i]);
+  A.k = k;
+  A.ctrl_set = op.ctrl_mask;
+  for (int j = 0; j < D; ++j)
+    for (int l = 0; l < k; ++l)
+      if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
+  A.units = uint64_t(1) << (nq - ins.size());
+  A.gpb = std::max(1, 256 / D);
+  const size_t smem = size_t(A.gpb) * D * sizeof(cplx_t<T>);
+  const uint64_t blocks = std::min<uint64_t>((A.units + A.gpb - 1) / A.gpb, uint64_t(num_sms()) * 8);
+  wide_kernel<T><<<unsigned(std::max<uint64_t>(1, blocks)), 256, smem, s>>>(
+      static_cast<cplx_t<T> *>(psi), static_cast<const cplx_t<T> *>(d_matrix), A);
+  return cudaGetLastError();
+}
+
+template <typename T>
 cudaError_t launch_dense_t(void *psi, unsigned nq, const DenseOp &op, cudaStream_t s) {
   T *tag = nullptr;
   switch (op.pos.size()) {
@@ -201,6 +270,12 @@ cudaError_t launch_dense_t(void *psi, unsigned nq, const DenseOp &op, cudaStream
 
 cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s) {
   return prec == 1 ? launch_dense_t<float>(psi, nq, op, s) : launch_dense_t<double>(psi, nq, op, s);
+}
+
+cudaError_t launch_wide(int prec, void *psi, unsigned nq, const DenseOp &op, const void *d_matrix,
+                        cudaStream_t s) {
+  if (op.pos.size() < 1 || op.pos.size() > 7) throw std::invalid_argument("wide gate kernel supports 1..7 targets");
+  return prec == 1 ? launch_wide_t<float>(psi, nq, op, d_matrix, s) : launch_wide_t<double>(psi, nq, op, d_matrix, s);
 }
 
 }  // namespace gsim
