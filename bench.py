@@ -66,6 +66,11 @@ def parse():
                     help="profiling mode: time one precision only (no accuracy, e2e or CPU legs)")
     ap.add_argument("--init", choices=["random", "zero"], default="random",
                     help="initial state; kernel times do not depend on the amplitudes")
+    ap.add_argument("--workload", choices=["circuit", "fused", "adjoint", "learned"], default="circuit",
+                    help="circuit: the 30-qubit headline; fused: k=5..7 dense gates at 32 qubits on tensor "
+                         "cores; adjoint: energy + gradient of a 960-parameter ansatz at 24 qubits; learned: "
+                         "learned vs greedy fusion planning on random circuits")
+    ap.add_argument("--ngates", type=int, default=60, help="fused workload: gates per step")
     return ap.parse_args()
 
 
@@ -277,6 +282,114 @@ def run_only(a):
                       "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
 
 
+def run_fused(a):
+    """Dense Haar-random k-qubit gates, k uniform in {5, 6, 7}, on a 32-qubit
+    complex64 state (32 GiB); targets always include a qubit below 5 and one
+    above 25.  k = 5, 6 run on tcgen05 tensor cores (3xTF32), k = 7 on the
+    shared-memory wide-gate kernel.  Error: the same gates at 24 qubits
+    against the complex128 path."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _circuits import haar_unitary
+    from projectq_gb300 import Simulator
+    from projectq_gb300.workloads import random_state
+
+    def gates_for(n, count, seed):
+        rng = np.random.default_rng(seed)
+        out = []
+        for _ in range(count):
+            k = int(rng.integers(5, 8))
+            low, high = int(rng.integers(0, 5)), int(rng.integers(n - 6, n))
+            rest = [int(q) for q in rng.permutation(n) if q not in (low, high)]
+            out.append((haar_unitary(k, rng), [low, high] + rest[: k - 2], []))
+        return out
+
+    nq = 32 if a.qubits == 30 else a.qubits
+    gates = gates_for(nq, a.ngates, 0)
+    sim = Simulator(1, precision="c64", fusion="staged")
+    for q in range(nq):
+        sim.allocate_qubit(q)
+    ms, cnt, recs = timed_steps(sim, gates, a.steps, a.warmup, None)
+    key, groups = dominant_kernel(recs)
+    flops = sum(8.0 * 2 ** nq * 2 ** len(t) for _, t, _ in gates) * a.steps
+    # accuracy at 24 qubits against complex128 (FP64 arithmetic)
+    small = gates_for(24, 30, 1)
+    res = {}
+    for prec in ("c64", "c128"):
+        s = Simulator(1, precision=prec, fusion="staged")
+        for q in range(24):
+            s.allocate_qubit(q)
+        s.set_wavefunction(random_state(24, seed=3), list(range(24)))
+        for m, t, c in small:
+            s.apply_controlled_gate(m, t, c)
+        s.run()
+        res[prec] = s
+    ip, maxerr = res["c128"].compare(res["c64"])
+    n1 = res["c128"].compare(res["c128"])[0].real
+    n2 = res["c64"].compare(res["c64"])[0].real
+    print(json.dumps({"workload": "fused k=5..7 dense gates", "qubits": nq, "gates_per_step": len(gates),
+                      "ms_per_step": ms / a.steps, "gates_per_s": len(gates) * a.steps / (ms * 1e-3),
+                      "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
+                      "hbm_gbs": cnt["gate_bytes"] / (ms * 1e-3) / 1e9,
+                      "accuracy_24q_30gates": {"one_minus_fidelity": 1 - abs(ip) ** 2 / (n1 * n2), "max_abs_err": maxerr},
+                      "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
+
+
+def run_adjoint(a):
+    """Energy and gradient of the hardware-efficient ansatz (20 layers of Ry,
+    Rz on each qubit + CNOT ladder: 960 parameters at 24 qubits) for a
+    200-term random Pauli Hamiltonian, by one adjoint sweep; checked against
+    central finite differences (h = 1e-4) on 8 parameters."""
+    from projectq_gb300 import Simulator
+    from projectq_gb300.adjoint import energy_and_gradient, hardware_efficient_ansatz
+    from projectq_gb300.workloads import random_pauli_hamiltonian
+
+    nq = 24 if a.qubits == 30 else a.qubits
+    circ = hardware_efficient_ansatz(nq, 20)
+    terms = random_pauli_hamiltonian(nq, 200, seed=0)
+    theta = np.random.default_rng(0).uniform(-np.pi, np.pi, size=circ.nparams)
+    out = {"workload": "adjoint gradient", "qubits": nq, "parameters": circ.nparams, "terms": len(terms)}
+    for prec in ("c128", "c64"):
+        sim = Simulator(1, precision=prec)
+        for q in range(nq):
+            sim.allocate_qubit(q)
+        for _ in range(max(1, a.warmup)):
+            energy_and_gradient(sim, circ, theta, terms, range(nq))
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            e, g = energy_and_gradient(sim, circ, theta, terms, range(nq))
+        dt = (time.perf_counter() - t0) / a.steps
+        rec = {"seconds_per_gradient": dt, "energy": e}
+        if prec == "c128":
+            h = 1e-4
+            idx = np.linspace(0, circ.nparams - 1, 8).astype(int)
+            fd = []
+            for j in idx:
+                tp, tm = theta.copy(), theta.copy()
+                tp[j] += h
+                tm[j] -= h
+                fd.append((energy_and_gradient(sim, circ, tp, terms, range(nq))[0]
+                           - energy_and_gradient(sim, circ, tm, terms, range(nq))[0]) / (2 * h))
+            fd = np.array(fd)
+            rec["fd_max_rel_err"] = float(np.max(np.abs(g[idx] - fd)) / max(1.0, np.max(np.abs(fd))))
+            g128 = g
+        else:
+            rec["max_abs_diff_vs_c128"] = float(np.max(np.abs(g - g128)))
+        out[prec] = rec
+    print(json.dumps(out), flush=True)
+
+
+def run_learned(a):
+    from projectq_gb300 import costmodel
+
+    res = costmodel.evaluate(costmodel.load_params(), ncirc=a.ngates, seed=7)
+    choices = {}
+    for r in res["rows"]:
+        choices[r["choice"]] = choices.get(r["choice"], 0) + 1
+    print(json.dumps({"workload": "learned vs greedy planning", "circuits": res["circuits"],
+                      "greedy_ms": res["greedy_ms"], "learned_ms": res["learned_ms"],
+                      "speedup": res["speedup"], "choices": choices}), flush=True)
+
+
 def main():
     a = parse()
     if a.impl == "reference":
@@ -284,6 +397,9 @@ def main():
         return
     if a.only:
         run_only(a)
+        return
+    if a.workload != "circuit":
+        {"fused": run_fused, "adjoint": run_adjoint, "learned": run_learned}[a.workload](a)
         return
     dist, world, rank, local = dist_init()
     from projectq_gb300 import Simulator

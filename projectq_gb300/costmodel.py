@@ -236,7 +236,7 @@ def main():
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
         np.savez(a.out, params=params, X=X, y=y)
     if a.evaluate and params is not None:
-        report["evaluation"] = {k: v for k, v in evaluate(params, a.evaluate).items() if k != "rows"}
+        report["evaluation"] = evaluate(params, a.evaluate)
     print(json.dumps(report))
 
 

@@ -276,8 +276,9 @@ class Engine {
     std::vector<cplx> M;
     std::vector<unsigned> ids, ctrls;
     fused_.compose(M, ids, ctrls);
-    if (ids.size() > max_gate_)
-      fail(GSIM_ERR_VALUE, "Gates with more than " + std::to_string(max_gate_) +
+    const unsigned limit = mode_ == GSIM_FUSION_REFERENCE ? max_gate_ : 7u;
+    if (ids.size() > limit)
+      fail(GSIM_ERR_VALUE, "Gates with more than " + std::to_string(limit) +
                                " qubits are not supported!");
     DenseOp op;
     op.m = std::move(M);
@@ -1371,10 +1372,13 @@ void Engine::run_learned() {
   int best = GSIM_FUSION_STAGED;
   float best_t = 0.f;
   bool first = true;
+  // The greedy (staged) plan is kept unless another plan is predicted to be
+  // at least 15% faster: small predicted gains are within the model's error.
+  const float penalty = -std::log(0.85f);  // added to the predicted log-time of the others
   for (int mode : {GSIM_FUSION_STAGED, GSIM_FUSION_REFERENCE, GSIM_FUSION_NONE}) {
     float f[kFeatures];
     plan_features_of(gates, mode, f, &staged);
-    const float t = predict(f);
+    const float t = predict(f) + (mode == GSIM_FUSION_STAGED ? 0.f : penalty);
     if (first || t < best_t) {
       best = mode;
       best_t = t;

@@ -382,6 +382,27 @@ class Simulator:
     def reset_counters(self):
         self._check(self._api.reset_counters(self._h))
 
+    def apply_gates(self, gates):
+        """Submit many gates in one call: [(matrix, target ids, control ids), ...]
+        (the same gates apply_controlled_gate takes, without per-gate ctypes
+        round trips for the matrix conversion)."""
+        for m, t, c in gates:
+            self.apply_controlled_gate(m, t, c)
+
+    def cuda_array(self):
+        """Zero-copy view of the flushed device state: an object with
+        __cuda_array_interface__ (wrap it with torch.as_tensor(view,
+        device="cuda") or cupy.asarray).  Valid until the qubit count changes."""
+        ptr, n, dt = self.device_state()
+
+        class _View:
+            __cuda_array_interface__ = {
+                "shape": (n,), "typestr": "<c8" if dt == "c64" else "<c16", "data": (ptr, False),
+                "version": 3, "strides": None,
+            }
+
+        return _View()
+
     def device_state(self):
         """(device pointer, number of amplitudes, "c64"|"c128") of the flushed state."""
         ptr = C.c_void_p()

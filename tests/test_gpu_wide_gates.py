@@ -56,6 +56,8 @@ def test_wide_gate_matches_numpy(prec, fusion, k):
 
 
 def test_reference_mode_keeps_the_five_qubit_limit():
+    """The reference engine rejects fused gates wider than 5 qubits at run()
+    (simulator.hpp:522); the reference planner mode keeps that behaviour."""
     sim = make("gpu", seed=1)
     allocate(sim, 8)
     sim.apply_controlled_gate(np.eye(64), list(range(6)), [])
