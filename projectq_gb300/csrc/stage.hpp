@@ -125,17 +125,53 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
   sp.subs.clear();
   sp.sops.clear();
   const unsigned L = sp.L;
-  size_t i = 0;
-  while (i < sp.ops.size()) {
+  const size_t nops = sp.ops.size();
+  // Qubits (global positions) each operation touches, for the commutation test:
+  // operations commute when they share no qubit, or when both are diagonal.
+  std::vector<uint64_t> touch(nops, 0);
+  std::vector<uint32_t> tmask(nops, 0);
+  for (size_t o = 0; o < nops; ++o) {
+    const StageOpDev &op = sp.ops[o];
+    for (unsigned q = 0; q < op.k; ++q)
+      touch[o] |= uint64_t(1) << (op.tbit[q] == 0xFF ? op.gbit[q] : sp.lpos[op.tbit[q]]);
+    if (op.kind == 0) {
+      for (unsigned q = 0; q < op.k; ++q) tmask[o] |= 1u << op.tbit[q];
+      for (unsigned b = 0; b < L; ++b)
+        if ((op.lctrl >> b) & 1) touch[o] |= uint64_t(1) << sp.lpos[b];
+      touch[o] |= op.gctrl;
+    }
+  }
+  std::vector<std::vector<size_t>> preds(nops);
+  for (size_t b = 0; b < nops; ++b)
+    for (size_t a = 0; a < b; ++a)
+      if ((touch[a] & touch[b]) && !(sp.ops[a].kind == 1 && sp.ops[b].kind == 1)) preds[b].push_back(a);
+  std::vector<char> done(nops, 0);
+  size_t ndone = 0;
+  while (ndone < nops) {
+    // List scheduling: take every ready operation that fits the register set.
     uint32_t R = 0;  // tile-bit mask
-    size_t j = i;
-    for (; j < sp.ops.size(); ++j) {
-      const StageOpDev &op = sp.ops[j];
-      if (op.kind == 1) continue;
-      uint32_t T = 0;
-      for (unsigned q = 0; q < op.k; ++q) T |= 1u << op.tbit[q];
-      if (unsigned(__builtin_popcount(R | T)) > r) break;
-      R |= T;
+    std::vector<size_t> chosen;
+    bool progress = true;
+    while (progress) {
+      progress = false;
+      for (size_t o = 0; o < nops; ++o) {
+        if (done[o]) continue;
+        bool ready = true;
+        for (size_t p : preds[o])
+          if (!done[p]) {
+            ready = false;
+            break;
+          }
+        if (!ready) continue;
+        if (sp.ops[o].kind == 0) {
+          if (unsigned(__builtin_popcount(R | tmask[o])) > r) continue;
+          R |= tmask[o];
+        }
+        done[o] = 1;
+        ++ndone;
+        chosen.push_back(o);
+        progress = true;
+      }
     }
     // Pad R to r bits, taking bits from the bank classes with most spare bits.
     while (unsigned(__builtin_popcount(R)) < r) {
@@ -183,7 +219,7 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
     auto row_index = [&](unsigned tb) {
       return int(std::find(rows.begin(), rows.end(), tb) - rows.begin());
     };
-    for (size_t o = i; o < j; ++o) {
+    for (size_t o : chosen) {
       const StageOpDev &op = sp.ops[o];
       SubOpDev so;
       std::memset(&so, 0, sizeof(so));
@@ -242,7 +278,6 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
     }
     sd.op_end = uint32_t(sp.sops.size());
     sp.subs.push_back(sd);
-    i = j;
   }
 }
 
