@@ -285,9 +285,9 @@ def run_only(a):
 def run_fused(a):
     """Dense Haar-random k-qubit gates, k uniform in {5, 6, 7}, on a 32-qubit
     complex64 state (32 GiB); targets always include a qubit below 5 and one
-    above 25.  k = 5, 6 run on tcgen05 tensor cores (3xTF32), k = 7 on the
-    shared-memory wide-gate kernel.  Error: the same gates at 24 qubits
-    against the complex128 path."""
+    above 25.  All run on the tcgen05 tensor-core kernel (3xTF32, FP32
+    accumulation).  Error: the same kind of gates at 24 qubits against the
+    complex128 path (FP64 arithmetic)."""
     sys.path.insert(0, str(ROOT / "tests"))
     from _circuits import haar_unitary
     from projectq_gb300 import Simulator
@@ -379,15 +379,22 @@ def run_adjoint(a):
 
 
 def run_learned(a):
+    """Learned fusion planner on a stream of random circuits (qubits uniform
+    in 20..30 complex64, depth 10..200, the config-5 gate mix, 10% ending
+    with the time evolution of a 50-term Pauli Hamiltonian): host wall time
+    with the shipped cost model against the greedy fixed-size fusion and the
+    stage planner, and 1 - F of the learned result against the greedy one."""
     from projectq_gb300 import costmodel
 
-    res = costmodel.evaluate(costmodel.load_params(), ncirc=a.ngates, seed=7)
+    shipped = costmodel.load()
+    res = costmodel.evaluate(shipped["params"], shipped["regimes_c64"], ncirc=a.ngates, seed=11)
     choices = {}
     for r in res["rows"]:
         choices[r["choice"]] = choices.get(r["choice"], 0) + 1
-    print(json.dumps({"workload": "learned vs greedy planning", "circuits": res["circuits"],
-                      "greedy_ms": res["greedy_ms"], "learned_ms": res["learned_ms"],
-                      "speedup": res["speedup"], "choices": choices}), flush=True)
+    rows = res.pop("rows")
+    print(json.dumps({"workload": "learned fusion planner vs greedy fixed-size fusion", **res, "choices": choices,
+                      "per_circuit": [{k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
+                                      for r in rows]}), flush=True)
 
 
 def main():

@@ -189,11 +189,13 @@ GSIM_API int gsim_state_device_ptr(gsim_engine *e, void **ptr, size_t *len, int 
 /* Wait for all work queued on the engine's stream. */
 GSIM_API int gsim_synchronize(gsim_engine *e);
 
-/* Select the fusion planner (GSIM_FUSION_*) and its widest fused gate. */
+/* Select the fusion planner (GSIM_FUSION_*).  kmax (0 = unchanged): for
+ * GSIM_FUSION_REFERENCE the widest cluster of the greedy rule (1..7; the
+ * reference's is 5); for GSIM_FUSION_STAGED values >= 6 set the tile width. */
 GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
 
 /* Use (on != 0, the default) or avoid the tcgen05 tensor-core kernel for
- * fused complex64 gates of 5 or 6 targets (3xTF32 split precision). */
+ * fused complex64 gates of 5 to 7 targets (3xTF32 split precision). */
 GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int on);
 
 /* Preallocate device memory for nqubits qubits (avoids regrowth). */
@@ -225,8 +227,9 @@ GSIM_API int gsim_timer_elapsed(gsim_engine *e, int a, int b, float *ms);
  * is bracketed by CUDA events on the engine's stream.  fetch waits for the
  * stream and copies up to cap records. */
 typedef struct gsim_launch_record {
-  uint32_t kind;      /* 0 dense gate kernel, 1 staged tile kernel */
-  uint32_t k;         /* matrix qubits */
+  uint32_t kind;      /* 0 dense gate kernel (CUDA cores, k <= 5), 1 stage kernel,
+                         2 wide gate kernel (k = 6, 7), 3 tensor-core gate kernel */
+  uint32_t k;         /* matrix qubits (stage kernel: operations in the stage) */
   uint32_t nctrl;     /* control qubits */
   uint32_t nqubits;   /* state qubits */
   uint64_t targets;   /* bit mask of the matrix qubits' positions */
@@ -234,7 +237,7 @@ typedef struct gsim_launch_record {
   uint32_t precision; /* GSIM_C128 or GSIM_C64 */
   uint32_t ngates;    /* logical gates applied by the launch */
   float ms;           /* device time of the launch */
-  float pad;
+  uint32_t aux;       /* stage kernel: register substages (0: one pass per operation) */
 } gsim_launch_record;
 GSIM_API int gsim_profile_enable(gsim_engine *e, int on);
 GSIM_API int gsim_profile_fetch(gsim_engine *e, gsim_launch_record *out, size_t cap, size_t *n);
@@ -266,15 +269,27 @@ GSIM_API int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *k
                                    double *energy, double *grad);
 
 /* ---- Learned fusion planner (no reference counterpart) ----------------------
- * gsim_plan_features: the 16 cost-model features of executing the queued
- * gates (staged / learned modes queue gates until run) with planner `mode`
- * (GSIM_FUSION_STAGED, _REFERENCE or _NONE), from a dry run of that planner.
+ * The cost model predicts log(milliseconds) of one kernel launch from 16
+ * features of it; GSIM_FUSION_LEARNED sums the predictions over three
+ * candidate plans of the queued gates (the greedy fixed-size clusters of
+ * the reference's rule, clusters whose boundaries the model chooses, the
+ * stage plan) and runs the cheapest.
+ * gsim_launch_features: the features of n launch records (out: n x nfeat,
+ * nfeat >= 16), the same function the planner applies to candidate launches;
+ * needs no engine and no GPU.
  * gsim_set_cost_model: install trained weights (nfeatures = 16, `hidden`
- * units per layer, layout of gsim_mlp_get_params) for GSIM_FUSION_LEARNED.
- * gsim_last_plan_choice: the planner the last learned flush used. */
-GSIM_API int gsim_plan_features(gsim_engine *e, int mode, float *out, size_t n);
+ * units per layer, layout of gsim_mlp_get_params).
+ * gsim_set_learned_regimes: allowed[n] != 0 lets learned plans run on
+ * n-qubit states (n < count <= 65); elsewhere, and without a cost model, the
+ * learned mode runs the greedy fixed-size fusion.
+ * gsim_last_plan_choice: the plan the last learned flush ran
+ * (GSIM_FUSION_REFERENCE greedy clusters, _STAGED, _LEARNED model clusters)
+ * and, when pred_ms is not NULL, the three predicted times (greedy, stage,
+ * model clusters) in milliseconds. */
+GSIM_API int gsim_launch_features(const gsim_launch_record *recs, size_t n, float *out, size_t nfeat);
 GSIM_API int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *params);
-GSIM_API int gsim_last_plan_choice(gsim_engine *e, int *mode);
+GSIM_API int gsim_set_learned_regimes(gsim_engine *e, const uint8_t *allowed, size_t count);
+GSIM_API int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms);
 
 /* The cost model's network: F inputs -> H -> H -> 1 (ReLU), FP32, with
  * hand-written forward, backward and Adam kernels (mlp.cu).  Parameters are

@@ -92,7 +92,7 @@ class LaunchRecord(C.Structure):
         ("precision", C.c_uint32),
         ("ngates", C.c_uint32),
         ("ms", C.c_float),
-        ("pad", C.c_float),
+        ("aux", C.c_uint32),
     ]
 
 
@@ -117,9 +117,10 @@ PRODUCT_ONLY = {
         [_eng, _sz, _u8p, _u32p, _u32p, _u32p, C.POINTER(C.c_int32), _f64p, _f64p, _sz, _u32p, _u32p, _u8p,
          _f64p, _sz, _u32p, _sz, C.c_uint32, _f64p, _f64p],
     ),
-    "plan_features": (C.c_int, [_eng, C.c_int, C.POINTER(C.c_float), _sz]),
+    "launch_features": (C.c_int, [C.POINTER(LaunchRecord), _sz, C.POINTER(C.c_float), _sz]),
     "set_cost_model": (C.c_int, [_eng, C.c_int, C.c_int, C.POINTER(C.c_float)]),
-    "last_plan_choice": (C.c_int, [_eng, C.POINTER(C.c_int)]),
+    "set_learned_regimes": (C.c_int, [_eng, _u8p, _sz]),
+    "last_plan_choice": (C.c_int, [_eng, C.POINTER(C.c_int), _f64p]),
     "mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_void_p)]),
     "mlp_destroy": (C.c_int, [C.c_void_p]),
     "mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(_sz)]),

@@ -1,21 +1,28 @@
 """Learned fusion cost model.
 
-The engine can execute a flush of queued gates with three planners: the
-shared-memory stage planner ("staged", the greedy default), the reference's
-dense-cluster rule ("reference") and one pass per gate ("none").  Which is
-fastest depends on the state size (a state that fits in L2 favours cheap
-per-gate passes), the gate mix and the precision.  The cost model is a 2x64
-ReLU MLP (hand-written CUDA forward/backward/Adam kernels, mlp.cu) that maps
-the 16 plan features of gsim_plan_features to log(milliseconds); with
-fusion="learned" the engine evaluates it for every planner at each flush and
-runs the plan with the lowest prediction.
+A 16 -> 64 -> 64 -> 1 ReLU MLP (hand-written CUDA forward / backward / Adam
+kernels, mlp.cu) predicts log(milliseconds) of ONE kernel launch from 16
+features of it (gsim_launch_features: kernel kind, targets k, controls,
+lowest target bit, targets inside a 128-byte line, bytes, flops, stage
+operations and substages, state size, whether the state fits in L2,
+precision).  It is trained on the per-launch timings the engine records with
+its profiler while running random circuits under several planners (greedy
+fixed-size clusters of width 2..7, one launch per gate, stage plans).
+
+With fusion="learned" the engine sums the predictions over three candidate
+plans of each flush -- the greedy fixed-size clusters of the reference's rule,
+clusters whose boundaries the model chooses (a gate joins the open cluster
+when the merged launch is predicted cheaper than two launches), and the
+stage plan -- and runs the cheapest.  The greedy fixed-size fusion is the
+fallback and the judge: `calibrate` measures wall time of learned against
+greedy per state size on circuits not used for training, and the engine
+runs learned plans only on the state sizes where they won
+(gsim_set_learned_regimes); everywhere else, and with no model installed,
+it runs the greedy fusion.
 
 Workflow (on the GPU):
-    python -m projectq_gb300.costmodel --collect 240 --train --evaluate 60 \
-        --out projectq_gb300/data/cost_model.npz
-which times random circuits of the learned-planner workload under each
-planner (engine CUDA events), trains on the recorded timings and reports the
-measured wall time of learned vs greedy planning on held-out circuits.
+    python -m projectq_gb300.costmodel --collect 60 --train --calibrate 3 \
+        --evaluate 24 --out projectq_gb300/data/cost_model.npz
 """
 
 from __future__ import annotations
@@ -31,12 +38,19 @@ import numpy as np
 
 from . import _lib
 from .simulator import Simulator
-from .workloads import Rz, Rx, Ry, X, Z
+from .workloads import Rz, Rx, Ry, X, Z, random_pauli_hamiltonian
 
 F = 16
 H = 64
-MODES = {"staged": _lib.GSIM_FUSION_STAGED, "reference": _lib.GSIM_FUSION_REFERENCE, "none": _lib.GSIM_FUSION_NONE}
 DATA = Path(__file__).resolve().parent / "data" / "cost_model.npz"
+# planners whose launches make up the training set: (fusion mode, kmax); the
+# learned clusters reach 7 qubits in complex64 and 5 in complex128
+COLLECT_PLANNERS = {
+    "c64": [("staged", 0), ("none", 0)] + [("reference", k) for k in (2, 3, 4, 5, 6, 7)],
+    "c128": [("staged", 0), ("none", 0)] + [("reference", k) for k in (2, 3, 4, 5)],
+}
+CHOICES = {_lib.GSIM_FUSION_REFERENCE: "greedy", _lib.GSIM_FUSION_STAGED: "staged",
+           _lib.GSIM_FUSION_LEARNED: "model clusters"}
 
 
 def _fp(a):
@@ -123,120 +137,228 @@ def random_circuit(rng, n, depth):
     return gates
 
 
-def plan_features(sim, mode):
-    out = np.zeros(F, dtype=np.float32)
-    _lib.check(sim._api, sim._api.plan_features(sim._h, MODES[mode], _fp(out), F))
-    return out
+def launch_features(records, api=None):
+    """Features (n x 16) of launch records (dicts of profile_records or
+    LaunchRecord structs), computed by the engine's own gsim_launch_features."""
+    api = api or _lib.load()
+    n = len(records)
+    buf = (_lib.LaunchRecord * max(1, n))()
+    for i, r in enumerate(records):
+        for f, _ in _lib.LaunchRecord._fields_:
+            setattr(buf[i], f, r[f] if isinstance(r, dict) else getattr(r, f))
+    out = np.zeros((max(1, n), F), dtype=np.float32)
+    _lib.check(api, api.launch_features(buf, n, _fp(out), F))
+    return out[:n]
 
 
-def features_for(n, gates, precision="c64"):
-    """Plan features of `gates` on n qubits under every planner."""
+def _new_sim(n, precision, fusion="staged", kmax=0):
     sim = Simulator(1, precision=precision, fusion="staged")
     for q in range(n):
         sim.allocate_qubit(q)
-    for m, t, c in gates:
-        sim.apply_controlled_gate(m, t, c)
-    feats = {mode: plan_features(sim, mode) for mode in MODES}
+    sim.set_fusion(fusion, kmax)
+    return sim
+
+
+def record_launches(n, gates, fusion, kmax=0, precision="c64"):
+    """Run `gates` once on n qubits with the given planner and return the
+    engine's per-launch records (kind, k, controls, targets, bytes, ms...)."""
+    sim = _new_sim(n, precision, fusion, kmax)
+    sim.profile(True)
+    sim.apply_gates(gates)
+    sim.run()
+    recs = sim.profile_records()
     sim.close()
-    return feats
+    return recs
 
 
-def time_plan(n, gates, fusion, precision="c64", repeats=1, cost_model=None):
-    """Device milliseconds to apply `gates` with the given planner (engine
-    CUDA events around submission and flush; the best of `repeats`)."""
-    sim = Simulator(1, precision=precision, fusion="staged")
-    for q in range(n):
-        sim.allocate_qubit(q)
-    if fusion == "learned":
-        install(sim, cost_model)
-    sim.set_fusion(fusion)
-    best = math.inf
-    for _ in range(repeats + 1):
-        sim.synchronize()
-        sim.timer_mark(0)
-        for m, t, c in gates:
-            sim.apply_controlled_gate(m, t, c)
-        sim.run()
-        sim.timer_mark(1)
-        ms = sim.timer_elapsed(0, 1)
-        best = min(best, ms)
-    choice = C.c_int(-1)
-    sim._api.last_plan_choice(sim._h, C.byref(choice))
-    sim.close()
-    return best, choice.value
+def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64", "c128")):
+    """Per-launch training set: features and log(ms) of every launch of
+    `ncirc` random circuits, each run under every planner of COLLECT_PLANNERS."""
+    rng = np.random.default_rng(seed)
+    feats, ys = [], []
+    for i in range(ncirc):
+        n = int(rng.integers(nmin, nmax + 1))
+        prec = precisions[i % len(precisions)]
+        if prec == "c128":
+            n = min(n, nmax - 1)
+        depth = int(rng.integers(dmin, dmax + 1))
+        gates = random_circuit(rng, n, depth)
+        for fusion, kmax in COLLECT_PLANNERS[prec]:
+            recs = record_launches(n, gates, fusion, kmax, prec)
+            feats.append(launch_features(recs))
+            ys.append(np.log(np.maximum(np.array([r["ms"] for r in recs], dtype=np.float64), 1e-4)))
+    return np.concatenate(feats), np.concatenate(ys).astype(np.float32)
 
 
-def install(sim, params):
-    """Install cost-model weights (array or path) into an engine."""
-    if params is None:
-        params = load_params()
+def aggregate(X, y):
+    """One sample per distinct feature vector (median log-time)."""
+    keys, inv = np.unique(X, axis=0, return_inverse=True)
+    inv = inv.reshape(-1)
+    out = np.zeros(len(keys), dtype=np.float32)
+    for j in range(len(keys)):
+        out[j] = np.median(y[inv == j])
+    return keys.astype(np.float32), out
+
+
+def install(sim, params=None, regimes=None):
+    """Install cost-model weights (default: the shipped model) and, when
+    given (default: the shipped table for the engine's precision), the
+    per-state-size regimes in which learned plans beat the greedy fusion."""
+    if params is None or regimes is None:
+        shipped = load()
+        params = shipped["params"] if params is None else params
+        if regimes is None:
+            regimes = shipped["regimes_" + sim.precision]
     p = np.ascontiguousarray(params, dtype=np.float32)
     _lib.check(sim._api, sim._api.set_cost_model(sim._h, F, H, _fp(p)))
+    if regimes is not False:
+        r = np.ascontiguousarray(regimes, dtype=np.uint8)
+        _lib.check(sim._api, sim._api.set_learned_regimes(sim._h, r.ctypes.data_as(C.POINTER(C.c_uint8)), r.size))
+
+
+def load(path=DATA):
+    d = np.load(path)
+    return {k: d[k] for k in d.files}
 
 
 def load_params(path=DATA):
-    return np.load(path)["params"]
+    return load(path)["params"]
 
 
-def collect(ncirc, seed=0, nmin=18, nmax=27, dmin=10, dmax=200):
+def last_choice(sim):
+    mode = C.c_int(-1)
+    pred = np.zeros(3, dtype=np.float64)
+    _lib.check(sim._api, sim._api.last_plan_choice(sim._h, C.byref(mode), pred.ctypes.data_as(C.POINTER(C.c_double))))
+    return mode.value, pred
+
+
+def wall_time(n, gates, fusion, precision="c64", params=None, regimes=None, tail=None, keep=False):
+    """Host wall time (s) of submitting `gates`, flushing and synchronising
+    on a fresh n-qubit engine (allocation excluded), with `tail` (a Pauli
+    Hamiltonian and time) applied as emulate_time_evolution after the gates."""
+    sim = _new_sim(n, precision)
+    if fusion == "learned":
+        install(sim, params, regimes)
+    sim.set_fusion(fusion)
+    sim.synchronize()
+    t0 = time.perf_counter()
+    sim.apply_gates(gates)
+    if tail is not None:
+        terms, t = tail
+        sim.emulate_time_evolution(terms, t, list(range(n)), [])
+    sim.run()
+    sim.synchronize()
+    dt = time.perf_counter() - t0
+    choice = last_choice(sim)[0] if fusion == "learned" else None
+    if keep:
+        return dt, choice, sim
+    sim.close()
+    return dt, choice
+
+
+def _stream(rng, n, dmin, dmax, p_tail=0.1):
+    depth = int(rng.integers(dmin, dmax + 1))
+    gates = random_circuit(rng, n, depth)
+    tail = None
+    if rng.uniform() < p_tail:
+        ham = random_pauli_hamiltonian(n, nterms=50, seed=int(rng.integers(1 << 30)))
+        terms = [(tuple(t), c) for t, c in ham if t]
+        tail = (terms, float(rng.uniform(0, 1)))
+    return gates, tail
+
+
+def calibrate(params, per_size=3, sizes=range(18, 31), precisions=("c64", "c128"), seed=7, dmin=10, dmax=120):
+    """The judge: per state size, total wall time of learned against greedy
+    fixed-size fusion on `per_size` random circuits (not the training ones);
+    returns {precision: uint8[65]} with 1 where learned was faster."""
+    out = {}
     rng = np.random.default_rng(seed)
-    X, y, meta = [], [], []
-    for i in range(ncirc):
-        n = int(rng.integers(nmin, nmax + 1))
-        depth = int(rng.integers(dmin, dmax + 1))
-        gates = random_circuit(rng, n, depth)
-        feats = features_for(n, gates)
-        for mode in MODES:
-            ms, _ = time_plan(n, gates, mode)
-            X.append(feats[mode])
-            y.append(math.log(max(ms, 1e-3)))
-            meta.append((i, n, depth, mode, ms))
-    return np.array(X, dtype=np.float32), np.array(y, dtype=np.float32), meta
+    for prec in precisions:
+        allowed = np.zeros(65, dtype=np.uint8)
+        for n in sizes:
+            if prec == "c128" and n > max(sizes) - 1:
+                continue
+            tg = tl = 0.0
+            for _ in range(per_size):
+                gates, _ = _stream(rng, n, dmin, dmax, p_tail=0.0)
+                tg += wall_time(n, gates, "reference", prec)[0]
+                tl += wall_time(n, gates, "learned", prec, params, regimes=np.ones(65, np.uint8))[0]
+            allowed[n] = 1 if tl < tg else 0
+        out[prec] = allowed
+    return out
 
 
-def evaluate(params, ncirc, seed=1, **kw):
-    """Measured device time of learned vs greedy (staged) planning on held-out
-    circuits; both plans apply the same gates."""
+def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=30, dmin=10, dmax=200, precision="c64",
+             with_staged=True, fidelity=True):
+    """Config-5 style stream of `ncirc` random circuits (10% end with the time
+    evolution of a 50-term Pauli Hamiltonian): wall time with the learned
+    planner against the greedy fixed-size fusion (and the stage planner), and
+    1 - F between the learned and the greedy final states."""
     rng = np.random.default_rng(seed)
     rows = []
     for _ in range(ncirc):
-        n = int(rng.integers(kw.get("nmin", 18), kw.get("nmax", 27) + 1))
-        depth = int(rng.integers(kw.get("dmin", 10), kw.get("dmax", 200) + 1))
-        gates = random_circuit(rng, n, depth)
-        t_greedy, _ = time_plan(n, gates, "staged")
-        t_learned, choice = time_plan(n, gates, "learned", cost_model=params)
-        rows.append({"n": n, "gates": len(gates), "greedy_ms": t_greedy, "learned_ms": t_learned, "choice": choice})
-    g = sum(r["greedy_ms"] for r in rows)
-    lrn = sum(r["learned_ms"] for r in rows)
-    return {"circuits": ncirc, "greedy_ms": g, "learned_ms": lrn, "speedup": g / lrn, "rows": rows}
+        n = int(rng.integers(nmin, nmax + 1))
+        gates, tail = _stream(rng, n, dmin, dmax)
+        tg, _, sg = wall_time(n, gates, "reference", precision, tail=tail, keep=True)
+        tl, choice, sl = wall_time(n, gates, "learned", precision, params, regimes, tail=tail, keep=True)
+        row = {"n": n, "gates": len(gates), "tail": tail is not None, "greedy_s": tg, "learned_s": tl,
+               "choice": CHOICES.get(choice, str(choice))}
+        if fidelity:
+            ip, err = sg.compare(sl)
+            n1, n2 = sg.compare(sg)[0].real, sl.compare(sl)[0].real
+            row["one_minus_fidelity"] = max(0.0, 1.0 - abs(ip) ** 2 / (n1 * n2))
+            row["max_abs_err"] = err
+        sg.close()
+        sl.close()
+        if with_staged:
+            row["staged_s"] = wall_time(n, gates, "staged", precision, tail=tail)[0]
+        rows.append(row)
+    res = {"circuits": ncirc, "precision": precision,
+           "greedy_s": sum(r["greedy_s"] for r in rows), "learned_s": sum(r["learned_s"] for r in rows)}
+    res["speedup_vs_greedy"] = res["greedy_s"] / res["learned_s"]
+    if with_staged:
+        res["staged_s"] = sum(r["staged_s"] for r in rows)
+        res["speedup_vs_staged"] = res["staged_s"] / res["learned_s"]
+    if fidelity:
+        res["max_one_minus_fidelity"] = max(r["one_minus_fidelity"] for r in rows)
+    res["rows"] = rows
+    return res
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--collect", type=int, default=240)
+    ap.add_argument("--collect", type=int, default=60)
     ap.add_argument("--train", action="store_true")
+    ap.add_argument("--epochs", type=int, default=4000)
+    ap.add_argument("--calibrate", type=int, default=0, help="circuits per state size for the judge")
     ap.add_argument("--evaluate", type=int, default=0)
-    ap.add_argument("--epochs", type=int, default=3000)
     ap.add_argument("--out", default=str(DATA))
     a = ap.parse_args()
     t0 = time.time()
-    X, y, meta = collect(a.collect)
-    report = {"samples": len(y), "collect_s": time.time() - t0}
-    params = None
+    X, y = collect(a.collect)
+    Xu, yu = aggregate(X, y)
+    report = {"launches": int(len(y)), "distinct": int(len(yu)), "collect_s": time.time() - t0}
     if a.train:
         net = MLP(seed=0)
-        n = len(y)
-        idx = np.random.default_rng(0).permutation(n)
-        cut = int(0.8 * n)
+        idx = np.random.default_rng(0).permutation(len(yu))
+        cut = int(0.85 * len(yu))
         tr, va = idx[:cut], idx[cut:]
-        loss = net.train(X[tr], y[tr], epochs=a.epochs)
-        pred = net.predict(X[va])
-        report.update(train_mse=loss, val_mse=float(np.mean((pred - y[va]) ** 2)))
+        loss = net.train(Xu[tr], yu[tr], epochs=a.epochs)
+        pred = net.predict(Xu[va])
+        report.update(train_mse=loss, val_mse=float(np.mean((pred - yu[va]) ** 2)))
         params = net.params
+        regimes = {"c64": np.ones(65, np.uint8), "c128": np.ones(65, np.uint8)}
+        if a.calibrate:
+            t1 = time.time()
+            regimes = calibrate(params, per_size=a.calibrate)
+            report["calibrate_s"] = time.time() - t1
+            report["learned_sizes"] = {p: [int(i) for i in np.nonzero(r)[0]] for p, r in regimes.items()}
         Path(a.out).parent.mkdir(parents=True, exist_ok=True)
-        np.savez(a.out, params=params, X=X, y=y)
-    if a.evaluate and params is not None:
-        report["evaluation"] = evaluate(params, a.evaluate)
+        np.savez(a.out, params=params, regimes_c64=regimes["c64"], regimes_c128=regimes["c128"])
+        if a.evaluate:
+            ev = evaluate(params, regimes["c64"], a.evaluate)
+            ev.pop("rows")
+            report["evaluation"] = ev
     print(json.dumps(report))
 
 

@@ -8,10 +8,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <complex>
 #include <cstring>
 #include <map>
+#include <unordered_map>
 #include <random>
 #include <set>
 #include <string>
@@ -115,9 +117,11 @@ class Engine {
     pinned_.release();
     upload_host_.release();
     if (upload_ev_) cudaEventDestroy(upload_ev_);
-    mat_dev_.release();
-    mat_host_.release();
-    if (mat_ev_) cudaEventDestroy(mat_ev_);
+    for (UploadSlot &sl : mslots_) {
+      sl.dev.release();
+      sl.host.release();
+      if (sl.ev) cudaEventDestroy(sl.ev);
+    }
     if (stream_) cudaStreamDestroy(stream_);
   }
 
@@ -276,7 +280,7 @@ class Engine {
     std::vector<cplx> M;
     std::vector<unsigned> ids, ctrls;
     fused_.compose(M, ids, ctrls);
-    const unsigned limit = mode_ == GSIM_FUSION_REFERENCE ? max_gate_ : 7u;
+    const unsigned limit = mode_ == GSIM_FUSION_REFERENCE ? std::max(max_gate_, fmax_) : 7u;
     if (ids.size() > limit)
       fail(GSIM_ERR_VALUE, "Gates with more than " + std::to_string(limit) +
                                " qubits are not supported!");
@@ -621,30 +625,37 @@ class Engine {
   }
 
   // ---- learned planner -----------------------------------------------------
-  // Features of executing the queued gates with planner `mode` (dry run):
-  // the cost model's input.  Only meaningful in the staged / learned modes,
-  // where gates are queued until run().
+  // The cost model maps the features of one kernel launch (launch_features)
+  // to its predicted log(milliseconds); the learned planner sums predictions
+  // over candidate plans of the queued gates.
   static constexpr int kFeatures = 16;
-  void plan_features(int mode, float *f) {
-    std::vector<StageGate> gates = queued_positions();
-    plan_features_of(gates, mode, f);
-  }
   void set_cost_model(int F, int H, const float *params) {
     if (F != kFeatures || H < 1 || H > 256) fail(GSIM_ERR_VALUE, "cost model: unexpected layer sizes");
     cm_H_ = H;
     cm_.assign(params, params + (size_t(H) * F + H + size_t(H) * H + H + H + 1));
+    memo_.clear();
+  }
+  // allowed[n] != 0: learned plans may run on an n-qubit state; elsewhere the
+  // greedy fixed-size fusion runs (regimes where measured wall time did not
+  // beat it).
+  void set_learned_regimes(const uint8_t *allowed, size_t n) {
+    learned_ok_.assign(65, 1);
+    for (size_t i = 0; i < std::min<size_t>(n, 65); ++i) learned_ok_[i] = allowed[i] ? 1 : 0;
   }
   int last_choice() const { return last_choice_; }
+  void last_prediction(double *out) const { std::copy(last_pred_, last_pred_ + 3, out); }
 
   void set_fusion(int mode, unsigned kmax) {
     run();
     if (mode != GSIM_FUSION_REFERENCE && mode != GSIM_FUSION_NONE && mode != GSIM_FUSION_STAGED &&
         mode != GSIM_FUSION_LEARNED)
       fail(GSIM_ERR_VALUE, "unknown fusion mode");
-    if (mode == GSIM_FUSION_LEARNED && cm_.empty())
-      fail(GSIM_ERR_VALUE, "the learned planner needs a cost model (gsim_set_cost_model)");
     mode_ = mode;
-    if (kmax) kmax_ = std::min(kmax, 5u);
+    if (mode == GSIM_FUSION_REFERENCE && kmax) {  // widest cluster of the greedy fixed-size rule
+      if (kmax > 7) fail(GSIM_ERR_VALUE, "set_fusion(): clusters of at most 7 qubits");
+      fmax_ = kmax;
+      fmin_ = std::min(4u, kmax);
+    }
     if (mode == GSIM_FUSION_STAGED && kmax >= 6) {  // kmax >= 6 selects the tile width in staged mode
       tile_bits_c64_ = std::min(kmax, 14u);
       tile_bits_c128_ = std::min(kmax - 1, 13u);
@@ -765,25 +776,19 @@ class Engine {
     int e0 = -1;
     if (profiling_) e0 = record_event();
     const size_t kq = op.pos.size();
-    if (prec_ == GSIM_C64 && use_tc_ && (kq == 5 || kq == 6) && N_ >= kq + 7) {
+    const int route = dense_kind(kq);
+    if (route == 3) {
       // tensor cores: U embedded as a real 2^(k+1) square matrix, TF32 hi/lo
-      std::vector<float> hi, lo;
-      tc_split_unitary(op.m, int(kq), hi, lo);
-      if (mat_ev_) CK(cudaEventSynchronize(mat_ev_));
-      const size_t nb = hi.size() * 4;
-      char *h = static_cast<char *>(mat_host_.get(2 * nb));
-      std::memcpy(h, hi.data(), nb);
-      std::memcpy(h + nb, lo.data(), nb);
-      char *d = static_cast<char *>(mat_dev_.get(2 * nb));
-      CK(cudaMemcpyAsync(d, h, 2 * nb, cudaMemcpyHostToDevice, stream_));
-      if (!mat_ev_) CK(cudaEventCreateWithFlags(&mat_ev_, cudaEventDisableTiming));
-      CK(cudaEventRecord(mat_ev_, stream_));
+      const size_t nb = tc_operand_floats(int(kq)) * 4;
+      char *h = nullptr;
+      UploadSlot &sl = next_slot(nb, h);
+      tc_prepare_operand(op.m, int(kq), reinterpret_cast<float *>(h));
+      const void *d = finish_slot(sl, h, nb);
       int *d_err = reinterpret_cast<int *>(static_cast<char *>(small_.get(4096)) + 2048);
       if (!tc_used_) CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
-      CK(launch_tc_gate(state_.p, N_, op, reinterpret_cast<const float *>(d),
-                        reinterpret_cast<const float *>(d + nb), d_err, stream_));
+      CK(launch_tc_gate(state_.p, N_, op, static_cast<const float *>(d), d_err, stream_));
       tc_used_ = true;
-    } else if (kq > 5) {
+    } else if (route == 2) {
       const size_t D = size_t(1) << op.pos.size();
       void *dm = upload_matrix(op.m, D * D);
       CK(launch_wide(prec_, state_.p, N_, op, dm, stream_));
@@ -794,7 +799,7 @@ class Engine {
       const int e1 = record_event();
       Prof p;
       std::memset(&p.rec, 0, sizeof(p.rec));
-      p.rec.kind = 0;
+      p.rec.kind = uint32_t(route);
       p.rec.k = uint32_t(op.pos.size());
       p.rec.nctrl = c;
       p.rec.nqubits = N_;
@@ -810,12 +815,33 @@ class Engine {
     counters_[2] += bytes;
     counters_[3] += 1;
   }
-  // Copy a matrix in the state's precision to device memory (a ring of
-  // buffers; the host staging buffer is reused only after its copy is done).
+  // A ring of upload slots (pinned host staging + device buffer): a slot's
+  // host buffer is rewritten only after its previous copy has run, so the
+  // host can prepare the next few matrices while earlier kernels execute.
+  struct UploadSlot {
+    DevBuf dev;
+    HostBuf host;
+    cudaEvent_t ev = nullptr;
+  };
+  UploadSlot &next_slot(size_t bytes, char *&h) {
+    UploadSlot &sl = mslots_[mslot_next_];
+    mslot_next_ = (mslot_next_ + 1) % mslots_.size();
+    if (sl.ev) CK(cudaEventSynchronize(sl.ev));
+    h = static_cast<char *>(sl.host.get(bytes));
+    sl.dev.get(bytes);
+    return sl;
+  }
+  void *finish_slot(UploadSlot &sl, const char *h, size_t bytes) {
+    CK(cudaMemcpyAsync(sl.dev.p, h, bytes, cudaMemcpyHostToDevice, stream_));
+    if (!sl.ev) CK(cudaEventCreateWithFlags(&sl.ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(sl.ev, stream_));
+    return sl.dev.p;
+  }
+  // Copy a matrix in the state's precision to device memory.
   void *upload_matrix(const std::vector<cplx> &m, size_t count) {
     const size_t bytes = count * bpa_;
-    if (mat_ev_) CK(cudaEventSynchronize(mat_ev_));
-    char *h = static_cast<char *>(mat_host_.get(bytes));
+    char *h = nullptr;
+    UploadSlot &sl = next_slot(bytes, h);
     for (size_t i = 0; i < count; ++i) {
       if (prec_ == GSIM_C64) {
         reinterpret_cast<float *>(h)[2 * i] = float(m[i].real());
@@ -825,11 +851,7 @@ class Engine {
         reinterpret_cast<double *>(h)[2 * i + 1] = m[i].imag();
       }
     }
-    void *d = mat_dev_.get(bytes);
-    CK(cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, stream_));
-    if (!mat_ev_) CK(cudaEventCreateWithFlags(&mat_ev_, cudaEventDisableTiming));
-    CK(cudaEventRecord(mat_ev_, stream_));
-    return d;
+    return finish_slot(sl, h, bytes);
   }
   int record_event() {
     if (ev_next_ >= ev_pool_.size()) {
@@ -847,12 +869,26 @@ class Engine {
   void execute_staged(std::vector<PlanStep> &steps);
   void exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool);
   void run_learned();
-  void reference_counts(const std::vector<StageGate> &gates, std::vector<std::pair<unsigned, unsigned>> &launches) const;
   std::vector<StageGate> queued_positions() const;
   std::vector<DenseOp> reference_plan(const std::vector<StageGate> &gates) const;
-  void plan_features_of(const std::vector<StageGate> &gates, int mode, float *f,
-                        const std::vector<PlanStep> *staged = nullptr) const;
+  // a cluster: gates [begin, end) fused into one dense launch on matrix
+  // qubits q with shared controls c (bit masks of positions)
+  struct Cluster {
+    size_t begin = 0, end = 0;
+    uint64_t q = 0, c = 0;
+  };
+  std::vector<Cluster> greedy_clusters(const std::vector<StageGate> &gates) const;
+  std::vector<Cluster> learned_clusters(const std::vector<StageGate> &gates);
+  gsim_launch_record dense_record(uint64_t q, uint64_t c) const;
+  double predict_ms(const gsim_launch_record &r);
+  double clusters_ms(const std::vector<Cluster> &cl);
+  double staged_ms(const std::vector<PlanStep> &steps);
+  void exec_clusters(std::vector<StageGate> &gates, const std::vector<Cluster> &cl);
   float predict(const float *f) const;
+  int dense_kind(size_t kq) const {
+    if (prec_ == GSIM_C64 && use_tc_ && kq >= 5 && kq <= 7 && N_ >= kq + 7) return 3;
+    return kq > 5 ? 2 : 0;
+  }
 
   double masked_norm_host(uint64_t mask, uint64_t val) {
     double *d_norm = static_cast<double *>(small_.get(4096));
@@ -936,19 +972,21 @@ class Engine {
   std::mt19937 rng_;
   std::uniform_real_distribution<double> dist_{0., 1.};
   RefFusion fused_;
-  unsigned fmin_ = 4, fmax_ = 5, max_gate_ = 5, kmax_ = 5;
+  unsigned fmin_ = 4, fmax_ = 5, max_gate_ = 5;
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
   unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
   bool tc_used_ = false;
-  DevBuf mat_dev_;
-  HostBuf mat_host_;
-  cudaEvent_t mat_ev_ = nullptr;
+  std::array<UploadSlot, 4> mslots_;
+  size_t mslot_next_ = 0;
   std::vector<float> cm_;  // cost-model weights (host copy)
   int cm_H_ = 0;
   int last_choice_ = -1;
+  std::vector<uint8_t> learned_ok_ = std::vector<uint8_t>(65, 1);
+  std::unordered_map<uint64_t, double> memo_;  // launch key -> predicted ms
+  double last_pred_[3] = {0, 0, 0};                // predicted ms: greedy, staged, learned clusters
   DevBuf upload_dev_;
   HostBuf upload_host_;
   cudaEvent_t upload_ev_ = nullptr;
@@ -1161,6 +1199,7 @@ void Engine::exec_stage(const StagePlan &sp, const void *d_ops, const void *d_po
     p.rec.bytes = bytes;
     p.rec.precision = uint32_t(prec_);
     p.rec.ngates = sp.ngates;
+    p.rec.aux = uint32_t(sp.subs.size());
     p.ev0 = e0;
     p.ev1 = e1;
     prof_.push_back(p);
@@ -1222,124 +1261,222 @@ std::vector<DenseOp> Engine::reference_plan(const std::vector<StageGate> &gates)
   return out;
 }
 
-// The reference's admission rule (simulator.hpp:204-222, fusion.hpp:130-160)
-// replayed on qubit sets only: (matrix qubits, shared controls) per launch.
-void Engine::reference_counts(const std::vector<StageGate> &gates,
-                              std::vector<std::pair<unsigned, unsigned>> &launches) const {
-  uint64_t qs = 0, cs = 0;
-  size_t items = 0;
-  auto flush = [&]() {
-    if (items) launches.emplace_back(unsigned(__builtin_popcountll(qs)), unsigned(__builtin_popcountll(cs)));
-    qs = cs = 0;
-    items = 0;
-  };
-  auto insert = [&](uint64_t &q, uint64_t &c, size_t &n, const StageGate &g) {
-    uint64_t t = 0;
-    for (unsigned p : g.pos) t |= uint64_t(1) << p;
-    q |= t;
-    uint64_t dropped = c & ~g.ctrl_mask;  // shared controls this gate lacks
-    const uint64_t fresh = g.ctrl_mask & ~c;
+namespace {
+// The reference's cluster admission (fusion.hpp:130-160) on qubit sets only:
+// add gate g to a cluster with matrix qubits q, shared controls c and n gates.
+void cluster_insert(uint64_t &q, uint64_t &c, size_t &n, const StageGate &g) {
+  uint64_t t = 0;
+  for (unsigned p : g.pos) t |= uint64_t(1) << p;
+  q |= t;
+  const uint64_t dropped = c & ~g.ctrl_mask;  // shared controls this gate lacks
+  const uint64_t fresh = g.ctrl_mask & ~c;
+  if (n) {
+    q |= fresh;  // new controls become matrix qubits
+  } else {
+    c |= fresh;
+  }
+  if (dropped) {
+    c &= ~dropped;
+    q |= dropped;
+  }
+  ++n;
+}
+constexpr double kLaunchGapMs = 0.002;  // host launch gap added per kernel launch
+}  // namespace
+
+// Features of one kernel launch: the cost model's input, shared by training
+// (recorded launches) and planning (candidate launches).
+void launch_features(const gsim_launch_record &r, float *f) {
+  std::fill(f, f + Engine::kFeatures, 0.f);
+  const double B = r.precision == GSIM_C64 ? 8.0 : 16.0;
+  const double amps = std::ldexp(1.0, int(r.nqubits));
+  auto lg = [](double x) { return float(std::log2(1.0 + x)); };
+  f[0] = float(r.nqubits) / 32.f;
+  f[1] = r.precision == GSIM_C64 ? 1.f : 0.f;
+  f[2 + std::min<uint32_t>(r.kind, 3u)] = 1.f;
+  double flops;
+  if (r.kind == 1) {  // stage: k = operations, aux = register substages (0: one pass per operation)
+    flops = amps * double(r.k);
+    f[12] = float(r.k) / 64.f;
+    f[13] = float(r.aux) / 32.f;
+  } else {
+    const double touched = std::ldexp(1.0, int(r.nqubits) - int(r.nctrl));
+    flops = touched * std::ldexp(1.0, int(r.k));
+    f[6] = float(r.k) / 8.f;
+    f[7] = float(r.nctrl) / 8.f;
+    f[8] = r.targets ? float(__builtin_ctzll(r.targets)) / 32.f : 0.f;
+    f[9] = float(__builtin_popcountll(r.targets & 0xFull)) / 4.f;
+  }
+  f[10] = lg(double(r.bytes)) / 48.f;
+  f[11] = lg(flops) / 48.f;
+  f[14] = amps * B <= 96e6 ? 1.f : 0.f;  // the state fits in L2
+  f[15] = 1.f;
+}
+
+// The greedy fixed-size fusion (simulator.hpp:204-222) as clusters.
+std::vector<Engine::Cluster> Engine::greedy_clusters(const std::vector<StageGate> &gates) const {
+  std::vector<Cluster> out;
+  Cluster cur;
+  size_t n = 0;
+  auto flush = [&](size_t end) {
     if (n) {
-      q |= fresh;  // new controls become matrix qubits
-    } else {
-      c |= fresh;
+      cur.end = end;
+      out.push_back(cur);
     }
-    if (dropped) {
-      c &= ~dropped;
-      q |= dropped;
-    }
-    ++n;
+    cur = Cluster();
+    cur.begin = end;
+    n = 0;
   };
-  for (auto const &g : gates) {
-    uint64_t q2 = qs, c2 = cs;
-    size_t n2 = items;
-    insert(q2, c2, n2, g);
+  for (size_t i = 0; i < gates.size(); ++i) {
+    const StageGate &g = gates[i];
+    uint64_t q2 = cur.q, c2 = cur.c;
+    size_t n2 = n;
+    cluster_insert(q2, c2, n2, g);
     const unsigned nf = unsigned(__builtin_popcountll(q2));
     const unsigned nt = unsigned(g.pos.size());
     if (nf >= fmin_ && nf <= fmax_) {
-      qs = q2;
-      cs = c2;
-      items = n2;
-      flush();
-    } else if (nf > fmax_ || (nf - nt) > unsigned(__builtin_popcountll(qs))) {
-      flush();
-      insert(qs, cs, items, g);
+      cur.q = q2, cur.c = c2, n = n2;
+      flush(i + 1);
+    } else if (nf > fmax_ || (nf - nt) > unsigned(__builtin_popcountll(cur.q))) {
+      flush(i);
+      cluster_insert(cur.q, cur.c, n, g);
     } else {
-      qs = q2;
-      cs = c2;
-      items = n2;
+      cur.q = q2, cur.c = c2, n = n2;
     }
   }
-  flush();
+  flush(gates.size());
+  return out;
 }
 
-// 16 features: state size, precision, gate count, the candidate planner and
-// the launches, bytes and arithmetic of its plan (all log-scaled).
-void Engine::plan_features_of(const std::vector<StageGate> &gates, int mode, float *f,
-                              const std::vector<PlanStep> *staged) const {
-  std::fill(f, f + kFeatures, 0.f);
-  const double B = double(bpa_);
-  double launches = 0, bytes = 0, flops = 0, ops = 0, subs = 0, wide = 0;
-  auto dense_cost = [&](const DenseOp &op) {
-    const unsigned c = unsigned(__builtin_popcountll(op.ctrl_mask));
-    const double touched = std::ldexp(1.0, int(N_) - int(c));
-    launches += 1;
-    bytes += 2 * touched * B;
-    flops += touched * double(size_t(1) << op.pos.size());
-    if (op.pos.size() >= 3) wide += 1;
-  };
-  if (mode == GSIM_FUSION_STAGED) {
-    std::vector<PlanStep> own;
-    if (!staged) {
-      own = plan_staged(gates);
-      staged = &own;
+gsim_launch_record Engine::dense_record(uint64_t q, uint64_t c) const {
+  gsim_launch_record r;
+  std::memset(&r, 0, sizeof(r));
+  const unsigned k = unsigned(__builtin_popcountll(q)), nc = unsigned(__builtin_popcountll(c));
+  r.kind = uint32_t(dense_kind(k));
+  r.k = k;
+  r.nctrl = nc;
+  r.nqubits = N_;
+  r.targets = q;
+  r.bytes = 2 * (uint64_t(1) << (N_ - nc)) * bpa_;
+  r.precision = uint32_t(prec_);
+  return r;
+}
+
+double Engine::predict_ms(const gsim_launch_record &r) {
+  // The features depend only on these fields (bytes follows from nqubits,
+  // nctrl and precision), so they key the memo of predictions.
+  const uint64_t lowt = r.targets ? uint64_t(__builtin_ctzll(r.targets)) : 0;
+  const uint64_t key = uint64_t(r.kind & 3u) | (uint64_t(r.k & 255u) << 2) | (uint64_t(r.nctrl & 63u) << 10) |
+                       (lowt << 16) | (uint64_t(__builtin_popcountll(r.targets & 0xFull)) << 22) |
+                       (uint64_t(r.nqubits & 63u) << 25) | (uint64_t(r.precision & 1u) << 31) |
+                       (uint64_t(r.aux & 0xFFFFu) << 32);
+  auto it = memo_.find(key);
+  if (it != memo_.end()) return it->second;
+  float f[kFeatures];
+  launch_features(r, f);
+  const double ms = std::exp(double(predict(f)));
+  memo_.emplace(key, ms);
+  return ms;
+}
+
+double Engine::clusters_ms(const std::vector<Cluster> &cl) {
+  double t = 0;
+  for (auto const &c : cl) t += predict_ms(dense_record(c.q, c.c)) + kLaunchGapMs;
+  return t;
+}
+
+double Engine::staged_ms(const std::vector<PlanStep> &steps) {
+  double t = 0;
+  for (auto const &st : steps) {
+    if (!st.is_stage) {
+      uint64_t q = 0;
+      for (unsigned p : st.dense.pos) q |= uint64_t(1) << p;
+      t += predict_ms(dense_record(q, st.dense.ctrl_mask)) + kLaunchGapMs;
+      continue;
     }
-    for (auto const &st : *staged) {
-      if (!st.is_stage) {
-        dense_cost(st.dense);
-        continue;
-      }
-      launches += 1;
-      bytes += 2 * std::ldexp(1.0, int(N_)) * B;
-      ops += double(st.stage.ops.size());
-      subs += double(st.stage.subs.size());
-      flops += std::ldexp(1.0, int(N_)) * double(st.stage.ops.size());
+    gsim_launch_record r;
+    std::memset(&r, 0, sizeof(r));
+    r.kind = 1;
+    r.k = uint32_t(st.stage.ops.size());
+    r.aux = uint32_t(st.stage.subs.size());
+    r.nqubits = N_;
+    r.bytes = 2 * (uint64_t(1) << N_) * bpa_;
+    r.precision = uint32_t(prec_);
+    t += predict_ms(r) + kLaunchGapMs;
+  }
+  return t;
+}
+
+// Cluster boundaries chosen by the cost model: walking the gates in order,
+// the next gate joins the open cluster when the predicted time of the merged
+// launch is below that of the open cluster plus the gate on its own (one
+// launch more); clusters hold at most 7 qubits in complex64 (tensor cores
+// from 5 targets up) and 5 in complex128 (FP64 on CUDA cores).
+std::vector<Engine::Cluster> Engine::learned_clusters(const std::vector<StageGate> &gates) {
+  const int cap = prec_ == GSIM_C64 ? 7 : 5;
+  std::vector<Cluster> out;
+  Cluster cur;
+  size_t n = 0;
+  for (size_t i = 0; i < gates.size(); ++i) {
+    const StageGate &g = gates[i];
+    if (n == 0) {
+      cur = Cluster();
+      cur.begin = i;
+      cur.end = i + 1;
+      cluster_insert(cur.q, cur.c, n, g);
+      continue;
     }
-  } else if (mode == GSIM_FUSION_REFERENCE) {
-    std::vector<std::pair<unsigned, unsigned>> ls;  // (matrix qubits, controls) per launch
-    reference_counts(gates, ls);
-    for (auto const &l : ls) {
-      const double touched = std::ldexp(1.0, int(N_) - int(l.second));
-      launches += 1;
-      bytes += 2 * touched * B;
-      flops += touched * std::ldexp(1.0, int(l.first));
-      if (l.first >= 3) wide += 1;
+    Cluster m = cur;
+    size_t n2 = n;
+    cluster_insert(m.q, m.c, n2, g);
+    m.end = i + 1;
+    bool merge = false;
+    if (__builtin_popcountll(m.q) <= cap) {
+      Cluster one;
+      size_t n1 = 0;
+      cluster_insert(one.q, one.c, n1, g);
+      const double t_merge = predict_ms(dense_record(m.q, m.c));
+      const double t_split = predict_ms(dense_record(cur.q, cur.c)) + predict_ms(dense_record(one.q, one.c)) +
+                             kLaunchGapMs;
+      merge = t_merge <= t_split;
     }
-  } else {
-    for (auto const &g : gates) {
-      DenseOp op;
-      op.pos = g.pos;
-      op.ctrl_mask = g.ctrl_mask;
-      dense_cost(op);
+    if (merge) {
+      cur = m;
+      n = n2;
+    } else {
+      out.push_back(cur);
+      cur = Cluster();
+      cur.begin = i;
+      cur.end = i + 1;
+      n = 0;
+      cluster_insert(cur.q, cur.c, n, g);
     }
   }
-  auto lg = [](double x) { return float(std::log2(1.0 + x)); };
-  f[0] = float(N_) / 32.f;
-  f[1] = prec_ == GSIM_C64 ? 1.f : 0.f;
-  f[2] = lg(double(gates.size())) / 16.f;
-  f[3] = mode == GSIM_FUSION_STAGED ? 1.f : 0.f;
-  f[4] = mode == GSIM_FUSION_REFERENCE ? 1.f : 0.f;
-  f[5] = mode == GSIM_FUSION_NONE ? 1.f : 0.f;
-  f[6] = lg(launches) / 16.f;
-  f[7] = lg(bytes) / 48.f;
-  f[8] = lg(flops) / 48.f;
-  f[9] = lg(ops) / 16.f;
-  f[10] = lg(subs) / 16.f;
-  f[11] = lg(wide) / 16.f;
-  f[12] = float(std::ldexp(1.0, int(N_)) * B <= 96e6);  // state fits in L2
-  f[13] = lg(bytes / std::max(1.0, launches)) / 48.f;
-  f[14] = float(launches / std::max<double>(1.0, double(gates.size())));
-  f[15] = 1.f;
+  if (n) out.push_back(cur);
+  return out;
+}
+
+// Compose each cluster's gates in order (the reference's fusion object,
+// positions used as ids) and launch it as one dense gate.
+void Engine::exec_clusters(std::vector<StageGate> &gates, const std::vector<Cluster> &cl) {
+  for (auto const &c : cl) {
+    RefFusion f;
+    for (size_t i = c.begin; i < c.end; ++i) {
+      std::vector<unsigned> ctrl;
+      for (unsigned b = 0; b < 64; ++b)
+        if ((gates[i].ctrl_mask >> b) & 1) ctrl.push_back(b);
+      f.insert(std::move(gates[i].m), gates[i].pos, ctrl);
+    }
+    std::vector<cplx> M;
+    std::vector<unsigned> q, cs;
+    f.compose(M, q, cs);
+    if (q.size() > 7) fail(GSIM_ERR_RUNTIME, "learned planner: cluster wider than 7 qubits");
+    DenseOp op;
+    op.m = std::move(M);
+    op.pos = q;
+    for (unsigned x : cs) op.ctrl_mask |= uint64_t(1) << x;
+    exec_dense(op);
+  }
 }
 
 float Engine::predict(const float *x) const {
@@ -1362,42 +1499,39 @@ float Engine::predict(const float *x) const {
   return s;
 }
 
-// GSIM_FUSION_LEARNED: predict the run time of the queued gates under each
-// planner and execute the cheapest plan.
+// GSIM_FUSION_LEARNED: the queued gates run as the plan with the lowest
+// predicted time among the greedy fixed-size clusters, the cost-model
+// clusters and the stage plan.  Without a cost model, or on a state size
+// where learned plans did not beat the greedy fusion in measured wall time,
+// the greedy fixed-size fusion runs.
 void Engine::run_learned() {
   if (queue_.empty()) return;
   std::vector<StageGate> gates = queued_positions();
   queue_.clear();
-  std::vector<PlanStep> staged = plan_staged(gates);
-  int best = GSIM_FUSION_STAGED;
-  float best_t = 0.f;
-  bool first = true;
-  // The greedy (staged) plan is kept unless another plan is predicted to be
-  // at least 15% faster: small predicted gains are within the model's error.
-  const float penalty = -std::log(0.85f);  // added to the predicted log-time of the others
-  for (int mode : {GSIM_FUSION_STAGED, GSIM_FUSION_REFERENCE, GSIM_FUSION_NONE}) {
-    float f[kFeatures];
-    plan_features_of(gates, mode, f, &staged);
-    const float t = predict(f) + (mode == GSIM_FUSION_STAGED ? 0.f : penalty);
-    if (first || t < best_t) {
-      best = mode;
-      best_t = t;
-      first = false;
-    }
+  if (cm_.empty() || !learned_ok_[std::min<unsigned>(N_, 64)]) {
+    for (auto const &op : reference_plan(gates)) exec_dense(op);
+    last_choice_ = GSIM_FUSION_REFERENCE;
+    return;
   }
+  std::vector<PlanStep> staged = plan_staged(gates);
+  const std::vector<Cluster> learned = learned_clusters(gates);
+  const double t_greedy = clusters_ms(greedy_clusters(gates));
+  const double t_staged = staged_ms(staged);
+  const double t_learned = clusters_ms(learned);
+  int best = GSIM_FUSION_REFERENCE;
+  double best_t = t_greedy;
+  if (t_staged < best_t) best = GSIM_FUSION_STAGED, best_t = t_staged;
+  if (t_learned < best_t) best = GSIM_FUSION_LEARNED, best_t = t_learned;
   last_choice_ = best;
+  last_pred_[0] = t_greedy;
+  last_pred_[1] = t_staged;
+  last_pred_[2] = t_learned;
   if (best == GSIM_FUSION_STAGED) {
     execute_staged(staged);
-  } else if (best == GSIM_FUSION_REFERENCE) {
-    for (auto const &op : reference_plan(gates)) exec_dense(op);
+  } else if (best == GSIM_FUSION_LEARNED) {
+    exec_clusters(gates, learned);
   } else {
-    for (auto &g : gates) {
-      DenseOp op;
-      op.m = std::move(g.m);
-      op.pos = g.pos;
-      op.ctrl_mask = g.ctrl_mask;
-      exec_dense(op);
-    }
+    for (auto const &op : reference_plan(gates)) exec_dense(op);
   }
 }
 
@@ -1765,17 +1899,31 @@ int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *kind, cons
 int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out) {
   return guard([&] { E(a)->compare(*E(b), out); });
 }
-int gsim_plan_features(gsim_engine *e, int mode, float *out, size_t n) {
+int gsim_launch_features(const gsim_launch_record *recs, size_t n, float *out, size_t nfeat) {
   return guard([&] {
-    if (n < size_t(Engine::kFeatures)) fail(GSIM_ERR_LENGTH, "plan_features(): output too small");
-    E(e)->plan_features(mode, out);
+    if (nfeat < size_t(Engine::kFeatures)) fail(GSIM_ERR_LENGTH, "launch_features(): nfeat < 16");
+    for (size_t i = 0; i < n; ++i) {
+      float f[Engine::kFeatures];
+      gsim::launch_features(recs[i], f);
+      std::fill(out + i * nfeat, out + (i + 1) * nfeat, 0.f);
+      std::copy(f, f + Engine::kFeatures, out + i * nfeat);
+    }
   });
 }
 int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *params) {
   return guard([&] { E(e)->set_cost_model(nfeatures, hidden, params); });
 }
-int gsim_last_plan_choice(gsim_engine *e, int *mode) {
-  return guard([&] { *mode = E(e)->last_choice(); });
+int gsim_set_learned_regimes(gsim_engine *e, const uint8_t *allowed, size_t count) {
+  return guard([&] {
+    if (count > 65) fail(GSIM_ERR_LENGTH, "set_learned_regimes(): at most 65 entries");
+    E(e)->set_learned_regimes(allowed, count);
+  });
+}
+int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms) {
+  return guard([&] {
+    *mode = E(e)->last_choice();
+    if (pred_ms) E(e)->last_prediction(pred_ms);
+  });
 }
 int gsim_set_tensor_cores(gsim_engine *e, int on) {
   return guard([&] { E(e)->set_tensor_cores(on != 0); });

@@ -14,12 +14,13 @@ namespace gsim {
 
 // prec: 0 = complex128 state, 1 = complex64 state.
 cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s);
-// Fused dense gates of 5 or 6 targets on a complex64 state with tcgen05
-// tensor cores (3xTF32).  d_bhi / d_blo: the real embedding of U split into
-// TF32 hi and lo parts (tc_split_unitary); *d_err is set on a timeout.
-void tc_split_unitary(const std::vector<cplx> &U, int k, std::vector<float> &hi, std::vector<float> &lo);
-cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_bhi, const float *d_blo,
-                           int *d_err, cudaStream_t s);
+// Fused dense gates of 5 to 7 targets on a complex64 state with tcgen05
+// tensor cores (3xTF32).  d_b: the real embedding of U split into TF32 hi and
+// lo parts, laid out by tc_prepare_operand (tc_operand_floats(k) floats);
+// *d_err is set when a wait inside the kernel times out.
+size_t tc_operand_floats(int k);
+void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out);
+cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s);
 // Gates of up to 7 targets; d_matrix: the 2^k x 2^k matrix (row-major) in the
 // state's precision in device memory.
 cudaError_t launch_wide(int prec, void *psi, unsigned nq, const DenseOp &op, const void *d_matrix,

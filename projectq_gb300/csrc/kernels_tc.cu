@@ -1,4 +1,4 @@
-// Fused dense k-qubit gates (k = 5, 6) on complex64 states with the 5th
+// Fused dense k-qubit gates (k = 5, 6, 7) on complex64 states with the 5th
 // generation tensor cores (tcgen05, TMEM accumulators), split-precision
 // 3xTF32 with FP32 accumulation.
 //
@@ -9,16 +9,27 @@
 //   B[2a][2j]   = Re U[a][j]   B[2a][2j+1]   = -Im U[a][j]
 //   B[2a+1][2j] = Im U[a][j]   B[2a+1][2j+1] =  Re U[a][j]
 // so D[g][2a], D[g][2a+1] are the real and imaginary parts of output a.
-// M = 128 groups (TMEM lanes), N = K = 2^(k+1).  Each operand is split in
-// shared memory into hi = tf32(x) and lo = tf32(x - hi); three MMAs per
-// K-step accumulate hi*hi + hi*lo + lo*hi.  B (the unitary) stays resident
-// in shared memory for the whole kernel; A is gathered from HBM in chunks
-// of 64 real components (32 amplitudes) per group.
+// M = 128 groups (TMEM lanes), N = K = 2^(k+1).  Each operand is split into
+// hi = tf32(x) and lo = tf32(x - hi); three MMAs per K-step accumulate
+// lo*hi + hi*lo + hi*hi.
 //
-// Roles: all 128 threads gather/split A and run the epilogue (thread t owns
-// group t = TMEM lane t); thread 0 issues the MMAs; completion is signalled
-// by tcgen05.commit on an mbarrier whose wait is bounded (on timeout the
-// kernel records an error code and frees TMEM before returning).
+// The kernel is persistent (one CTA per SM) and warp-specialised:
+//   warps 0-7   producers: gather 16 amplitudes of a group per K-chunk from
+//               HBM (two threads per group, loads of the next chunk issued
+//               before the current one is converted), split them into TF32
+//               hi/lo and write both into a ring of shared-memory stages;
+//   warps 8-11  epilogue: read a finished accumulator from TMEM
+//               (tcgen05.ld, warp w owns TMEM lanes 32*(w%4)..) and store the
+//               outputs back in place;
+//   warp 12     MMA issue (one thread): tcgen05.mma per K-step, tcgen05.commit
+//               to release a stage and to publish an accumulator;
+//   warp 13     (k = 7 only) streams the unitary's K-chunk for each stage
+//               into shared memory with cp.async.bulk; for k <= 6 the whole
+//               operand B stays resident.
+// Two TMEM accumulators let the epilogue of one tile overlap the MMAs of the
+// next.  Every mbarrier wait is bounded: on timeout the thread records an
+// error code, raises a CTA-wide abort flag that the other waits poll, and
+// all threads meet at the end where TMEM is freed.
 // Shared-memory operands use the canonical K-major, no-swizzle layout:
 // 8-row x 16-byte core matrices; LBO = core stride along K, SBO = stride
 // between 8-row groups.
@@ -35,14 +46,39 @@
 namespace gsim {
 namespace {
 
-constexpr int kKC = 64;  // real K components per A chunk
+constexpr int kRows = 128;         // groups per tile (MMA M, TMEM lanes)
+constexpr int kKC = 32;            // real K components per chunk (16 amplitudes)
+constexpr int kAmpsPerChunk = kKC / 2;
+constexpr int kProducers = 256;    // warps 0-7
+constexpr int kEpilogue = 128;     // warps 8-11
+constexpr int kMmaWarp = 12;
+constexpr int kLoaderWarp = 13;
+constexpr int kPrefetch = 4;       // K-chunks of loads in flight per producer thread
+constexpr uint32_t kStageA = uint32_t(kRows) * kKC * 4u;  // one split (hi or lo) of an A chunk
+
+template <int KQ>
+struct TcCfg {
+  static constexpr int D = 1 << KQ;
+  static constexpr int K = 2 * D;
+  static constexpr int N = K;
+  static constexpr int NCH = K / kKC;
+  static constexpr bool kStream = KQ >= 7;  // B streamed per chunk instead of resident
+  static constexpr int S = KQ == 5 ? 4 : (KQ == 6 ? 3 : 2);
+  static constexpr uint32_t kStageB = kStream ? uint32_t(N) * kKC * 4u : 0u;  // one split of a B chunk
+  static constexpr uint32_t kBResident = kStream ? 0u : uint32_t(N) * K * 4u;  // one split of all of B
+  static constexpr uint32_t kStageBytes = 2 * kStageA + 2 * kStageB;
+  static constexpr uint32_t kBarOff = 2 * kBResident + S * kStageBytes;
+  static constexpr uint32_t kSmem = kBarOff + 256;
+  static constexpr int kThreads = kStream ? 448 : 416;
+  static constexpr uint32_t kTmemCols = 2u * N < 32u ? 32u : 2u * N;
+};
 
 struct TcArgs {
   uint64_t groups;      // number of amplitude groups
   uint64_t ctrl_set;
   int nins, k;
   uint8_t ins[64];
-  uint64_t off[64];     // offset of amplitude j of a group (j < 2^k, k <= 6)
+  uint64_t off[128];    // offset of amplitude j of a group (j < 2^k, k <= 7)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -57,7 +93,7 @@ __device__ __forceinline__ float tf32_round(float x) {
 
 // Byte offset of element (row, kk) in a K-major no-swizzle operand whose rows
 // hold kcols fp32 elements.
-__device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t kk, uint32_t kcols) {
+__host__ __device__ __forceinline__ uint32_t kmajor_off(uint32_t row, uint32_t kk, uint32_t kcols) {
   return ((row >> 3) * (kcols >> 2) + (kk >> 2)) * 128u + (row & 7u) * 16u + (kk & 3u) * 4u;
 }
 
@@ -84,24 +120,69 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
                : "memory");
 }
 
-// Bounded wait for the mbarrier phase `parity`; false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 24); ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(done)
-        : "r"(mbar), "r"(parity)
-        : "memory");
-    if (done) return true;
-    if (it > 1024) __nanosleep(64);
+__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar)
+      : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint32_t mbar, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(mbar),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t mbar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(done)
+      : "r"(mbar), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s: far above any legitimate wait
+
+// Bounded wait for the mbarrier phase `parity`.  Gives up (false) when the
+// CTA's abort flag is raised or after kWaitLimitNs of wall time (measured on
+// the global timer, so the bound holds however long one try_wait suspends),
+// in which case it records the error and raises the abort flag itself.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity, volatile int *abort_flag, int *err) {
+  if (mbar_try(mbar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (;;) {
+    if (mbar_try(mbar, parity)) return true;
+    if (*abort_flag) return false;
+    if (global_ns() - t0 > kWaitLimitNs) break;
   }
+  *abort_flag = 1;
+  atomicExch(err, 1);
   return false;
 }
 
-template <int NCOL>
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+      "l"(src), "r"(bytes), "r"(mbar)
+      : "memory");
+}
+
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   uint32_t r[16];
   asm volatile(
@@ -114,39 +195,81 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// K = N = 2^(k+1); B (N x K, hi and lo) resident; A chunks of 128 x kKC.
-template <int KQ>
-__global__ void __launch_bounds__(128, 1) tc_gate_kernel(float2 *__restrict__ psi, const float *__restrict__ b_hi,
-                                                         const float *__restrict__ b_lo,
-                                                         const __grid_constant__ TcArgs A, int *err) {
-  constexpr int D = 1 << KQ;       // complex dimension
-  constexpr int K = 2 * D;         // real K (= N)
-  constexpr int N = K;
-  constexpr int NCH = K / kKC;     // A chunks per tile
-  constexpr uint32_t A_BYTES = 128u * kKC * 4u;
-  constexpr uint32_t B_BYTES = uint32_t(N) * K * 4u;
-  extern __shared__ __align__(1024) unsigned char sm[];
-  unsigned char *a_hi = sm, *a_lo = sm + A_BYTES, *bh = sm + 2 * A_BYTES, *bl = bh + B_BYTES;
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(bl + B_BYTES);
-  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mbar + 1);
-  __shared__ int abort_flag;
+__device__ __forceinline__ uint64_t group_base(const TcArgs &A, uint64_t g) {
+  return insert_zeros(g, A.ins, A.nins) | A.ctrl_set;
+}
 
-  const int tid = threadIdx.x, warp = tid >> 5;
-  // B: copy the pre-split unitary into the K-major core layout.
-  for (int e = tid; e < N * K; e += 128) {
-    const int c = e / K, kk = e % K;
-    const uint32_t o = kmajor_off(uint32_t(c), uint32_t(kk), uint32_t(K));
-    *reinterpret_cast<float *>(bh + o) = b_hi[e];
-    *reinterpret_cast<float *>(bl + o) = b_lo[e];
+// Producer: one K-chunk (8 amplitudes of one group) into registers.
+template <int KQ>
+__device__ __forceinline__ void gather8(const float2 *__restrict__ psi, const TcArgs &A, uint64_t base, bool active,
+                                        int ch, int half, float2 (&x)[8]) {
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int j = ch * kAmpsPerChunk + half * 8 + q;
+    x[q] = active ? psi[base + A.off[j]] : make_float2(0.f, 0.f);
+  }
+}
+
+// Producer: split 8 amplitudes into TF32 hi/lo and store them as 4 pairs of
+// 16-byte core-matrix rows (K components 4p..4p+3 of this chunk).
+__device__ __forceinline__ void split_store(unsigned char *st, int row, int half, const float2 (&x)[8]) {
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    const float2 a = x[2 * p], b = x[2 * p + 1];
+    float4 h, l;
+    h.x = tf32_round(a.x);
+    h.y = tf32_round(a.y);
+    h.z = tf32_round(b.x);
+    h.w = tf32_round(b.y);
+    l.x = tf32_round(a.x - h.x);
+    l.y = tf32_round(a.y - h.y);
+    l.z = tf32_round(b.x - h.z);
+    l.w = tf32_round(b.y - h.w);
+    const uint32_t o = kmajor_off(uint32_t(row), uint32_t(half * 16 + 4 * p), uint32_t(kKC));
+    *reinterpret_cast<float4 *>(st + o) = h;
+    *reinterpret_cast<float4 *>(st + kStageA + o) = l;
+  }
+}
+
+template <int KQ>
+__global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
+    tc_gate_kernel(float2 *__restrict__ psi, const float *__restrict__ bsrc, const __grid_constant__ TcArgs A,
+                   int *err) {
+  using Cfg = TcCfg<KQ>;
+  constexpr int N = Cfg::N, K = Cfg::K, NCH = Cfg::NCH, S = Cfg::S;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  unsigned char *bres = sm;                             // resident B: hi then lo (k <= 6)
+  unsigned char *stages = sm + 2 * Cfg::kBResident;    // S x [A hi | A lo | B hi | B lo]
+  uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Cfg::kBarOff);
+  // bars: full[S], empty[S], accf[2], acce[2], drain
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 2 * S + 5);
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 6);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accf0 = smem_u32(bars + 2 * S),
+                 acce0 = smem_u32(bars + 2 * S + 2), drain = smem_u32(bars + 2 * S + 4);
+
+  if constexpr (!Cfg::kStream) {
+    const uint4 *src = reinterpret_cast<const uint4 *>(bsrc);
+    uint4 *dst = reinterpret_cast<uint4 *>(bres);
+    for (uint32_t e = tid; e < 2 * Cfg::kBResident / 16; e += blockDim.x) dst[e] = __ldg(src + e);
   }
   if (tid == 0) {
-    abort_flag = 0;
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(mbar)) : "memory");
+    *abort_flag = 0;
+    for (int s = 0; s < S; ++s) {
+      mbar_init(full0 + 8 * s, kProducers + (Cfg::kStream ? 1 : 0));
+      mbar_init(empty0 + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(accf0 + 8 * b, 1);
+      mbar_init(acce0 + 8 * b, kEpilogue);
+    }
+    mbar_init(drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(uint32_t(N < 32 ? 32 : N))
+                 "r"(Cfg::kTmemCols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -154,91 +277,179 @@ __global__ void __launch_bounds__(128, 1) tc_gate_kernel(float2 *__restrict__ ps
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t mb = smem_u32(mbar);
-  // idesc: D = F32, A = B = TF32, both K-major, N >> 3, M >> 4 (M = 128).
-  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(128 >> 4) << 24);
-  const uint32_t ahi_a = smem_u32(a_hi), alo_a = smem_u32(a_lo), bh_a = smem_u32(bh), bl_a = smem_u32(bl);
-  uint32_t phase = 0;
-  const uint64_t ntiles = (A.groups + 127) / 128;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const uint64_t g = tile * 128 + uint64_t(tid);
-    const bool active = g < A.groups;
-    const uint64_t base = active ? (insert_zeros(g, A.ins, A.nins) | A.ctrl_set) : 0;
-    for (int ch = 0; ch < NCH; ++ch) {
-      // gather + split this chunk of 32 amplitudes (64 real components)
-#pragma unroll 8
-      for (int jj = 0; jj < kKC / 2; ++jj) {
-        const int j = ch * (kKC / 2) + jj;
-        float2 x = make_float2(0.f, 0.f);
-        if (active) x = __ldcs(psi + base + A.off[j]);
-        const float hr = tf32_round(x.x), hi_ = tf32_round(x.y);
-        const float lr = tf32_round(x.x - hr), li = tf32_round(x.y - hi_);
-        const uint32_t o0 = kmajor_off(uint32_t(tid), uint32_t(2 * jj), kKC);
-        const uint32_t o1 = kmajor_off(uint32_t(tid), uint32_t(2 * jj + 1), kKC);
-        *reinterpret_cast<float *>(a_hi + o0) = hr;
-        *reinterpret_cast<float *>(a_hi + o1) = hi_;
-        *reinterpret_cast<float *>(a_lo + o0) = lr;
-        *reinterpret_cast<float *>(a_lo + o1) = li;
+  const uint64_t ntiles = (A.groups + kRows - 1) / kRows;
+
+  if (warp < kProducers / 32) {
+    // ---- producers -------------------------------------------------------
+    // A load cursor runs kPrefetch chunks ahead of the publish cursor: the
+    // registers of a chunk are refilled right after it was published, so
+    // about kPrefetch x 8 loads per thread are in flight.
+    const int row = tid & (kRows - 1), half = tid >> 7;
+    const uint64_t mine = blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+    const uint64_t total = mine * NCH;
+    uint64_t lt = blockIdx.x, loaded = 0;
+    int lc = 0;
+    bool lact = false;
+    uint64_t lbase = 0;
+    if (total) {
+      const uint64_t g = lt * kRows + uint64_t(row);
+      lact = g < A.groups;
+      lbase = lact ? group_base(A, g) : 0;
+    }
+    auto load_next = [&](float2 (&x)[8]) {
+      if (loaded >= total) return;
+      gather8<KQ>(psi, A, lbase, lact, lc, half, x);
+      ++loaded;
+      if (++lc == NCH) {
+        lc = 0;
+        lt += gridDim.x;
+        if (lt < ntiles) {
+          const uint64_t g = lt * kRows + uint64_t(row);
+          lact = g < A.groups;
+          lbase = lact ? group_base(A, g) : 0;
+        }
       }
+    };
+    uint64_t it = 0;
+    auto publish = [&](const float2 (&x)[8]) -> bool {
+      const int s = int(it % S);
+      const uint32_t u = uint32_t(it / S);
+      if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1u, abort_flag, err)) return false;
+      split_store(stages + size_t(s) * Cfg::kStageBytes, row, half, x);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (abort_flag) break;
-      if (tid == 0) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll 1
-        for (int s = 0; s < kKC / 8; ++s) {
-          // K-step s of this chunk: A cores 2s, 2s+1; B cores at the global K offset
-          const uint32_t ak = uint32_t(2 * s) * 128u;
-          const uint32_t bk = uint32_t(ch * (kKC / 4) + 2 * s) * 128u;
-          const uint64_t dah = smem_desc(ahi_a + ak, 128u, (kKC / 4) * 128u);
-          const uint64_t dal = smem_desc(alo_a + ak, 128u, (kKC / 4) * 128u);
-          const uint64_t dbh = smem_desc(bh_a + bk, 128u, (K / 4) * 128u);
-          const uint64_t dbl = smem_desc(bl_a + bk, 128u, (K / 4) * 128u);
-          const uint32_t acc0 = (ch > 0 || s > 0) ? 1u : 0u;
-          mma_tf32(tmem, dal, dbh, idesc, acc0);
-          mma_tf32(tmem, dah, dbl, idesc, 1u);
-          mma_tf32(tmem, dah, dbh, idesc, 1u);
-        }
-        mma_commit(mb);
-      }
-      if (!mbar_wait(mb, phase)) {
-        if (tid == 0) atomicExch(err, 1);
-        abort_flag = 1;
-      }
-      phase ^= 1u;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      __syncthreads();
-      if (abort_flag) break;
-    }
-    if (abort_flag) break;
-    // epilogue: TMEM lane (32 warp + lane) = group; N fp32 columns = D complex outputs
-    const uint32_t lane_base = uint32_t(warp * 32) << 16;
-#pragma unroll 1
-    for (int c0 = 0; c0 < N; c0 += 16) {
-      float v[16];
-      tmem_ld16<16>(tmem + lane_base + uint32_t(c0), v);
-      if (active) {
+      mbar_arrive(full0 + 8 * s);
+      ++it;
+      return true;
+    };
+    float2 x[kPrefetch][8];
 #pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int a = c0 / 2 + q;
-          __stcs(psi + base + A.off[a], make_float2(v[2 * q], v[2 * q + 1]));
+    for (int b = 0; b < kPrefetch; ++b) load_next(x[b]);
+    bool ok = true;
+    while (ok && it < total) {
+#pragma unroll
+      for (int b = 0; b < kPrefetch; ++b) {
+        if (it >= total) break;
+        if (!publish(x[b])) {
+          ok = false;
+          break;
+        }
+        load_next(x[b]);
+      }
+    }
+  } else if (warp < (kProducers + kEpilogue) / 32) {
+    // ---- epilogue --------------------------------------------------------
+    const int row = 32 * (warp & 3) + lane;
+    const uint32_t lane_base = uint32_t(32 * (warp & 3)) << 16;
+    uint32_t i = 0;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const uint32_t b = i & 1u, u = i >> 1;
+      if (!mbar_wait(accf0 + 8 * b, u & 1u, abort_flag, err)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint64_t g = tile * kRows + uint64_t(row);
+      const bool active = g < A.groups;
+      const uint64_t base = active ? group_base(A, g) : 0;
+#pragma unroll 1
+      for (int c0 = 0; c0 < N; c0 += 16) {
+        float v[16];
+        tmem_ld16(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+        if (active) {
+#pragma unroll
+          for (int q = 0; q < 8; ++q) __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(acce0 + 8 * b);
+    }
+  } else if (warp == kMmaWarp) {
+    // ---- MMA issue -------------------------------------------------------
+    if (lane == 0) {
+      // idesc: D = F32, A = B = TF32, both K-major, N >> 3, M >> 4 (M = 128).
+      const uint32_t idesc =
+          (1u << 4) | (2u << 7) | (2u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(kRows >> 4) << 24);
+      const uint32_t st0 = smem_u32(stages), br = smem_u32(bres);
+      uint64_t it = 0;
+      uint32_t i = 0;
+      bool ok = true;
+      for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++i) {
+        const uint32_t b = i & 1u, u = i >> 1;
+        if (u > 0 && !mbar_wait(acce0 + 8 * b, (u - 1) & 1u, abort_flag, err)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t dcol = tmem + b * uint32_t(N);
+        for (int ch = 0; ch < NCH; ++ch, ++it) {
+          const int s = int(it % S);
+          if (!mbar_wait(full0 + 8 * s, uint32_t(it / S) & 1u, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t sa = st0 + uint32_t(s) * Cfg::kStageBytes;
+#pragma unroll
+          for (int ks = 0; ks < kKC / 8; ++ks) {
+            const uint32_t ak = uint32_t(2 * ks) * 128u;
+            const uint64_t dah = smem_desc(sa + ak, 128u, (kKC / 4) * 128u);
+            const uint64_t dal = smem_desc(sa + kStageA + ak, 128u, (kKC / 4) * 128u);
+            uint64_t dbh, dbl;
+            if constexpr (Cfg::kStream) {
+              const uint32_t sb = sa + 2 * kStageA;
+              dbh = smem_desc(sb + ak, 128u, (kKC / 4) * 128u);
+              dbl = smem_desc(sb + Cfg::kStageB + ak, 128u, (kKC / 4) * 128u);
+            } else {
+              const uint32_t bk = uint32_t(ch * (kKC / 4) + 2 * ks) * 128u;
+              dbh = smem_desc(br + bk, 128u, (K / 4) * 128u);
+              dbl = smem_desc(br + Cfg::kBResident + bk, 128u, (K / 4) * 128u);
+            }
+            const uint32_t acc0 = (ch > 0 || ks > 0) ? 1u : 0u;
+            mma_tf32(dcol, dal, dbh, idesc, acc0);
+            mma_tf32(dcol, dah, dbl, idesc, 1u);
+            mma_tf32(dcol, dah, dbh, idesc, 1u);
+          }
+          mma_commit(empty0 + 8 * s);
+        }
+        if (!ok) break;
+        mma_commit(accf0 + 8 * b);
+      }
+    }
+  } else if (Cfg::kStream && warp == kLoaderWarp) {
+    // ---- B chunk loader (k = 7) --------------------------------------------
+    if (lane == 0) {
+      const uint32_t st0 = smem_u32(stages);
+      const char *src = reinterpret_cast<const char *>(bsrc);
+      uint64_t it = 0;
+      bool ok = true;
+      for (uint64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int ch = 0; ch < NCH; ++ch, ++it) {
+          const int s = int(it % S);
+          const uint32_t u = uint32_t(it / S);
+          if (u > 0 && !mbar_wait(empty0 + 8 * s, (u - 1) & 1u, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          const uint32_t dst = st0 + uint32_t(s) * Cfg::kStageBytes + 2 * kStageA;
+          mbar_arrive_tx(full0 + 8 * s, 2 * Cfg::kStageB);
+          bulk_g2s(dst, src + size_t(ch) * 2 * Cfg::kStageB, 2 * Cfg::kStageB, full0 + 8 * s);
         }
       }
     }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-    __syncthreads();
   }
+  // Before TMEM is freed every MMA must have completed: one more commit
+  // tracks all MMAs this thread issued (also after an abort).
+  if (warp == kMmaWarp && lane == 0) {
+    mma_commit(drain);
+    const uint64_t t0 = global_ns();
+    while (!mbar_try(drain, 0u) && global_ns() - t0 < kWaitLimitNs) {
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (warp == 0)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(uint32_t(N < 32 ? 32 : N))
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(Cfg::kTmemCols)
                  : "memory");
 }
 
 template <int KQ>
-cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_bhi, const float *d_blo,
-                        int *d_err, cudaStream_t s) {
-  constexpr int D = 1 << KQ, K = 2 * D, N = K;
+cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
+  using Cfg = TcCfg<KQ>;
   TcArgs A;
   std::memset(&A, 0, sizeof(A));
   std::vector<unsigned> ins(op.pos.begin(), op.pos.end());
@@ -250,32 +461,36 @@ cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *
   for (size_t i = 0; i < ins.size(); ++i) A.ins[i] = uint8_t(ins[i]);
   A.k = KQ;
   A.ctrl_set = op.ctrl_mask;
-  for (int j = 0; j < D; ++j)
+  for (int j = 0; j < Cfg::D; ++j)
     for (int l = 0; l < KQ; ++l)
       if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
   A.groups = uint64_t(1) << (nq - ins.size());
-  const size_t smem = 2 * size_t(128) * kKC * 4 + 2 * size_t(N) * K * 4 + 16;
   static bool attr = false;
   if (!attr) {
-    cudaFuncSetAttribute(tc_gate_kernel<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = cudaFuncSetAttribute(tc_gate_kernel<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(Cfg::kSmem));
+    if (e != cudaSuccess) return e;
     attr = true;
   }
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const uint64_t ntiles = (A.groups + 127) / 128;
+  const uint64_t ntiles = (A.groups + kRows - 1) / kRows;
   const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(sms))));
-  tc_gate_kernel<KQ><<<grid, 128, smem, s>>>(static_cast<float2 *>(psi), d_bhi, d_blo, A, d_err);
+  tc_gate_kernel<KQ><<<grid, Cfg::kThreads, Cfg::kSmem, s>>>(static_cast<float2 *>(psi), d_b, A, d_err);
   return cudaGetLastError();
 }
 
 }  // namespace
 
-// B operand (N x K row-major real embedding of U, split hi/lo in TF32) on the host.
-void tc_split_unitary(const std::vector<cplx> &U, int k, std::vector<float> &hi, std::vector<float> &lo) {
-  const int D = 1 << k, K = 2 * D;
-  hi.assign(size_t(K) * K, 0.f);
-  lo.assign(size_t(K) * K, 0.f);
+size_t tc_operand_floats(int k) { return size_t(2) * size_t(2 << k) * size_t(2 << k); }
+
+// Operand B (the real embedding of U, split hi/lo in TF32) laid out in the
+// shared-memory core-matrix order the kernel consumes:
+//   k <= 6: [hi: N x K][lo: N x K]                      (copied once per CTA)
+//   k = 7:  for each K-chunk: [hi: N x kKC][lo: N x kKC] (one bulk copy per stage)
+void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out) {
+  const int D = 1 << k, K = 2 * D, N = K;
   auto tf32 = [](float x) {  // round to nearest (ties away), 10 explicit mantissa bits
     uint32_t u;
     std::memcpy(&u, &x, 4);
@@ -283,6 +498,21 @@ void tc_split_unitary(const std::vector<cplx> &U, int k, std::vector<float> &hi,
     float r;
     std::memcpy(&r, &u, 4);
     return r;
+  };
+  const bool stream = k >= 7;
+  auto place = [&](int row, int col, float h, float l) {
+    size_t o;
+    size_t split;
+    if (!stream) {
+      o = kmajor_off(uint32_t(row), uint32_t(col), uint32_t(K)) / 4;
+      split = size_t(N) * K;
+    } else {
+      const int ch = col / kKC, kk = col % kKC;
+      o = size_t(ch) * 2 * N * kKC + kmajor_off(uint32_t(row), uint32_t(kk), uint32_t(kKC)) / 4;
+      split = size_t(N) * kKC;
+    }
+    out[o] = h;
+    out[o + split] = l;
   };
   for (int a = 0; a < D; ++a)
     for (int j = 0; j < D; ++j) {
@@ -292,18 +522,17 @@ void tc_split_unitary(const std::vector<cplx> &U, int k, std::vector<float> &hi,
       for (int t = 0; t < 4; ++t) {
         const float h = tf32(float(vals[t]));
         const float l = tf32(float(vals[t] - double(h)));
-        hi[size_t(rows[t]) * K + cols[t]] = h;
-        lo[size_t(rows[t]) * K + cols[t]] = l;
+        place(rows[t], cols[t], h, l);
       }
     }
 }
 
-cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_bhi, const float *d_blo,
-                           int *d_err, cudaStream_t s) {
+cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
   switch (op.pos.size()) {
-    case 5: return launch_tc_k<5>(psi, nq, op, d_bhi, d_blo, d_err, s);
-    case 6: return launch_tc_k<6>(psi, nq, op, d_bhi, d_blo, d_err, s);
-    default: throw std::invalid_argument("tensor-core gate kernel supports 5 or 6 targets");
+    case 5: return launch_tc_k<5>(psi, nq, op, d_b, d_err, s);
+    case 6: return launch_tc_k<6>(psi, nq, op, d_b, d_err, s);
+    case 7: return launch_tc_k<7>(psi, nq, op, d_b, d_err, s);
+    default: throw std::invalid_argument("tensor-core gate kernel supports 5 to 7 targets");
   }
 }
 

@@ -58,3 +58,31 @@ def test_no_gpu_is_an_error_status_not_a_crash(lib):
     assert b"device" in api.last_error()
     with pytest.raises(RuntimeError):
         _lib.check(api, rc)
+
+
+def test_launch_features_of_recorded_launches():
+    """gsim_launch_features needs no GPU: the cost model's inputs for a dense
+    launch and a stage launch, field by field."""
+    import math
+
+    import numpy as np
+
+    from projectq_gb300 import costmodel as cm
+
+    dense = {"kind": 0, "k": 2, "nctrl": 1, "nqubits": 20, "targets": 0b1010, "bytes": 2 * (1 << 19) * 8,
+             "precision": _lib.GSIM_C64, "ngates": 3, "ms": 0.1, "aux": 0}
+    stage = {"kind": 1, "k": 24, "nctrl": 0, "nqubits": 30, "targets": 0, "bytes": 2 * (1 << 30) * 16,
+             "precision": _lib.GSIM_C128, "ngates": 30, "ms": 9.0, "aux": 5}
+    f = cm.launch_features([dense, stage])
+    assert f.shape == (2, cm.F)
+    d, s = f
+    assert d[0] == pytest.approx(20 / 32) and d[1] == 1 and d[2] == 1 and d[3:6].sum() == 0
+    assert d[6] == pytest.approx(2 / 8) and d[7] == pytest.approx(1 / 8)
+    assert d[8] == pytest.approx(1 / 32) and d[9] == pytest.approx(2 / 4)
+    assert d[10] == pytest.approx(math.log2(1 + dense["bytes"]) / 48, rel=1e-6)
+    assert d[11] == pytest.approx(math.log2(1 + 2.0 ** 19 * 4) / 48, rel=1e-6)
+    assert d[14] == 1 and d[15] == 1
+    assert s[1] == 0 and s[3] == 1 and s[6] == 0 and s[12] == pytest.approx(24 / 64)
+    assert s[13] == pytest.approx(5 / 32) and s[14] == 0
+    assert s[11] == pytest.approx(math.log2(1 + 2.0 ** 30 * 24) / 48, rel=1e-6)
+    assert np.all(np.isfinite(f))

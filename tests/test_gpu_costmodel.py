@@ -70,39 +70,79 @@ def test_training_fits_a_smooth_target():
 
 
 def test_learned_planner_applies_the_same_gates():
+    """Whatever plan the model picks (here: untrained weights), the learned
+    mode applies the same gates: states agree with every other planner."""
     n = 14
     rng = np.random.default_rng(2)
     gates = cm.random_circuit(rng, n, 30)
-    params = cm.MLP(seed=5).params  # any weights: the choice must not change results
     states = {}
-    for mode in ("staged", "learned", "reference", "none"):
+    for seed in (5, 6):
+        params = cm.MLP(seed=seed).params
         s = make("gpu", seed=1, precision="c64", fusion="staged")
         allocate(s, n)
-        if mode == "learned":
-            cm.install(s, params)
-        s.set_fusion(mode)
-        for m, t, c in gates:
-            s.apply_controlled_gate(m, t, c)
+        cm.install(s, params, regimes=np.ones(65, np.uint8))
+        s.set_fusion("learned")
+        s.apply_gates(gates)
+        s.run()
+        states[f"learned{seed}"] = s.cheat()[1]
+    for mode in ("staged", "reference", "none"):
+        s = make("gpu", seed=1, precision="c64", fusion=mode)
+        allocate(s, n)
+        s.apply_gates(gates)
         s.run()
         states[mode] = s.cheat()[1]
-    for mode in ("learned", "reference", "none"):
+    for mode in ("learned5", "learned6", "reference", "none"):
         assert np.max(np.abs(states[mode] - states["staged"])) < 5e-6
 
 
-def test_plan_features_describe_each_planner():
-    n = 16
+def test_recorded_launches_carry_the_planner_features():
+    """Profiling records of each planner map to features of the right kernel
+    kind: greedy clusters of width k are dense launches with f[6] = k/8,
+    stages are kind 1 with their operation and substage counts."""
+    n = 20
     gates = cm.random_circuit(np.random.default_rng(3), n, 20)
-    f = cm.features_for(n, gates)
-    assert f["staged"][3] == 1 and f["reference"][4] == 1 and f["none"][5] == 1
-    # one pass per gate: launches/gates = 1; the stage planner needs far fewer passes
-    assert f["none"][14] == pytest.approx(1.0)
-    assert f["staged"][14] < 0.3
+    recs = cm.record_launches(n, gates, "reference", 3)
+    f = cm.launch_features(recs)
+    assert len(recs) > 0 and all(r["ms"] > 0 for r in recs)
+    for r, x in zip(recs, f):
+        assert x[2 + r["kind"]] == 1 and x[6] == pytest.approx(r["k"] / 8) and r["k"] <= 3
+    recs = cm.record_launches(n, gates, "staged")
+    f = cm.launch_features(recs)
+    st = [(r, x) for r, x in zip(recs, f) if r["kind"] == 1]
+    assert st and all(x[12] == pytest.approx(r["k"] / 64) and x[13] == pytest.approx(r["aux"] / 32) for r, x in st)
+
+
+def test_without_a_model_learned_mode_runs_the_greedy_fusion():
+    n = 16
+    gates = cm.random_circuit(np.random.default_rng(4), n, 10)
+    s = make("gpu", seed=1, precision="c64", fusion="learned")
+    allocate(s, n)
+    s.apply_gates(gates)
+    s.run()
+    assert cm.last_choice(s)[0] == 0  # GSIM_FUSION_REFERENCE
+    # a model with every regime disabled falls back the same way
+    s2 = make("gpu", seed=1, precision="c64", fusion="staged")
+    allocate(s2, n)
+    cm.install(s2, cm.MLP(seed=1).params, regimes=np.zeros(65, np.uint8))
+    s2.set_fusion("learned")
+    s2.apply_gates(gates)
+    s2.run()
+    assert cm.last_choice(s2)[0] == 0
+    assert np.max(np.abs(s.cheat()[1] - s2.cheat()[1])) < 1e-6
 
 
 @pytest.mark.skipif(not cm.DATA.exists(), reason="no trained cost model shipped")
-def test_shipped_cost_model_is_not_slower_than_greedy():
-    """Held-out circuits of the learned-planner workload: the plans the
-    trained model picks take no more device time than the greedy planner's
-    (5% timing noise allowed); the gain is reported in the assertion text."""
-    res = cm.evaluate(cm.load_params(), ncirc=12, seed=123, nmin=18, nmax=24, dmin=10, dmax=80)
-    assert res["learned_ms"] <= 1.05 * res["greedy_ms"], res
+def test_shipped_cost_model_beats_greedy_fusion():
+    """What the trained network gains over the method without it: held-out
+    circuits of the learned-planner workload (24-28 qubits, complex64 and
+    complex128) run in less wall time with the learned planner than with the
+    greedy fixed-size fusion, and the states agree (1 - F <= 1e-9 in
+    complex64, 1e-12 in complex128, F normalised by both norms).  The
+    measured gain is in the assertion message."""
+    shipped = cm.load()
+    for prec in ("c64", "c128"):
+        res = cm.evaluate(shipped["params"], shipped["regimes_" + prec], ncirc=4, seed=123, nmin=24, nmax=27,
+                          dmin=20, dmax=60, precision=prec, with_staged=False)
+        msg = {k: v for k, v in res.items() if k != "rows"}
+        assert res["learned_s"] < res["greedy_s"] / 1.2, msg
+        assert res["max_one_minus_fidelity"] <= (1e-9 if prec == "c64" else 1e-12), msg

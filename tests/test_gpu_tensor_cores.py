@@ -1,8 +1,10 @@
-"""Fused 5- and 6-qubit gates on complex64 states through the tcgen05
+"""Fused 5-, 6- and 7-qubit gates on complex64 states through the tcgen05
 tensor-core kernel (3xTF32, FP32 accumulation), against the complex128 path
 (FP64 arithmetic) and against complex64 on CUDA cores.  The gates are
 Haar-random with targets spanning low and high bit positions, with and
-without controls.  Tolerance: max |d psi| 5e-6 and 1 - F 1e-10."""
+without controls.  Sizes cover a partial tile (fewer than 128 groups), one
+tile, and many tiles per CTA (the stage ring and both TMEM accumulators
+wrap many times).  Tolerance: max |d psi| 5e-6 and 1 - F 1e-10."""
 
 import numpy as np
 import pytest
@@ -25,10 +27,9 @@ def run(prec, tc, n, psi, gates):
     return s.cheat()[1]
 
 
-@pytest.mark.parametrize("k", [5, 6])
-def test_tensor_core_gates_match_fp64(k):
-    n = 15
-    rng = np.random.default_rng(40 + k)
+@pytest.mark.parametrize("k,n", [(5, 13), (5, 15), (6, 15), (7, 15), (5, 24), (6, 23), (7, 22)])
+def test_tensor_core_gates_match_fp64(k, n):
+    rng = np.random.default_rng(40 + k + n)
     psi = random_state(n, seed=k)
     gates = []
     for trial in range(4):
