@@ -165,10 +165,11 @@ __global__ void __launch_bounds__(256) stage_kernel(cplx_t<T> *__restrict__ psi,
 }
 
 // ---- register substages (stage.hpp: build_substages) ----------------------
-__device__ __forceinline__ uint32_t swz(uint32_t p, uint32_t rho) {
+// s(p) = p ^ fold(p >> rho) is linear over XOR: s(a ^ b) = s(a) ^ s(b), so a
+// thread's offsets are its own s(.) XOR compile-time constants.
+__host__ __device__ constexpr uint32_t swz(uint32_t p, uint32_t rho) {
   uint32_t x = p >> rho, f = 0;
   const uint32_t mask = (1u << rho) - 1;
-#pragma unroll 1
   while (x) {
     f ^= x & mask;
     x >>= rho;
@@ -191,13 +192,15 @@ __device__ __forceinline__ void cmac_k(int kd, cplx_t<T> m, cplx_t<T> v, T &re, 
 // One 1-qubit operation on register bit B, matrix class CLS (stage.hpp):
 // 0 general complex, 1 real, 2 real diagonal / imaginary off-diagonal,
 // 4 anti-diagonal.  `amask` selects the group bases j the operation touches.
-template <typename T, int R, int B, int CLS>
+// FULL: every group base is active (no controls among the register bits), so
+// the per-base mask test is compiled out and the groups form one basic block.
+template <typename T, int R, int B, int CLS, bool FULL>
 __device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], uint32_t amask, const cplx_t<T> *M) {
   const cplx_t<T> m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if ((j >> B) & 1) continue;
-    if (!((amask >> j) & 1)) continue;
+    if (!FULL && !((amask >> j) & 1)) continue;
     const cplx_t<T> a = v[j], b = v[j | (1 << B)];
     T r0, i0, r1, i1;
     if constexpr (CLS == 1) {
@@ -226,33 +229,48 @@ __device__ __forceinline__ void reg_dense1(cplx_t<T> (&v)[1 << R], uint32_t amas
   }
 }
 
-template <typename T, int R, int B>
-__device__ __forceinline__ void reg_dense1_cls(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+template <typename T, int R, int B, bool FULL>
+__device__ __forceinline__ void reg_dense1_cls_f(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
   switch (op.cls) {
-    case 1: reg_dense1<T, R, B, 1>(v, op.amask, M); break;
-    case 2: reg_dense1<T, R, B, 2>(v, op.amask, M); break;
-    case 4: reg_dense1<T, R, B, 4>(v, op.amask, M); break;
-    default: reg_dense1<T, R, B, 0>(v, op.amask, M); break;
+    case 1: reg_dense1<T, R, B, 1, FULL>(v, op.amask, M); break;
+    case 2: reg_dense1<T, R, B, 2, FULL>(v, op.amask, M); break;
+    case 4: reg_dense1<T, R, B, 4, FULL>(v, op.amask, M); break;
+    default: reg_dense1<T, R, B, 0, FULL>(v, op.amask, M); break;
   }
 }
 
 template <typename T, int R, int B>
-__device__ __forceinline__ void reg_swap(cplx_t<T> (&v)[1 << R], uint32_t amask) {
+__device__ __forceinline__ void reg_dense1_cls(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
+  if (op.afull)
+    reg_dense1_cls_f<T, R, B, true>(v, op, M);
+  else
+    reg_dense1_cls_f<T, R, B, false>(v, op, M);
+}
+
+template <typename T, int R, int B, bool FULL>
+__device__ __forceinline__ void reg_swap_f(cplx_t<T> (&v)[1 << R], uint32_t amask) {
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if ((j >> B) & 1) continue;
-    if (!((amask >> j) & 1)) continue;
+    if (!FULL && !((amask >> j) & 1)) continue;
     const cplx_t<T> a = v[j];
     v[j] = v[j | (1 << B)];
     v[j | (1 << B)] = a;
   }
 }
 
+template <typename T, int R, int B>
+__device__ __forceinline__ void reg_swap(cplx_t<T> (&v)[1 << R], const SubOpDev &op) {
+  if (op.afull)
+    reg_swap_f<T, R, B, true>(v, op.amask);
+  else
+    reg_swap_f<T, R, B, false>(v, op.amask);
+}
+
 template <typename T, int R, int B0, int B1>
 __device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDev &op, const cplx_t<T> *M) {
-  cplx_t<T> mm[16];
-#pragma unroll
-  for (int e = 0; e < 16; ++e) mm[e] = M[e];
+  // matrix rows are re-read from shared memory (broadcast) per group rather
+  // than held in 32 registers: this path sets the kernel's register budget
 #pragma unroll
   for (int j = 0; j < (1 << R); ++j) {
     if (((j >> B0) & 1) || ((j >> B1) & 1)) continue;
@@ -264,7 +282,7 @@ __device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDe
     for (int a = 0; a < 4; ++a) {
       T re = T(0), im = T(0);
 #pragma unroll
-      for (int b = 0; b < 4; ++b) cfma<T>(mm[a * 4 + b], x[b], re, im);
+      for (int b = 0; b < 4; ++b) cfma<T>(M[a * 4 + b], x[b], re, im);
       y[a] = mkc<T>(re, im);
     }
     v[j] = y[0];
@@ -272,6 +290,13 @@ __device__ __forceinline__ void reg_dense2(cplx_t<T> (&v)[1 << R], const SubOpDe
     v[j2] = y[2];
     v[j3] = y[3];
   }
+}
+
+// Diagonal with one register qubit (register bit B): two factors.
+template <typename T, int R, int B>
+__device__ __forceinline__ void reg_diag1(cplx_t<T> (&v)[1 << R], cplx_t<T> f0, cplx_t<T> f1) {
+#pragma unroll
+  for (int j = 0; j < (1 << R); ++j) v[j] = cmul<T>(v[j], ((j >> B) & 1) ? f1 : f0);
 }
 
 template <typename T, int R>
@@ -283,6 +308,22 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
     for (int q = 0; q < int(op.dk); ++q) {
       if (op.dloc[q] == 1) cidx |= ((row >> op.didx[q]) & 1u) << q;
       else if (op.dloc[q] == 2) cidx |= uint32_t((base >> op.didx[q]) & 1) << q;
+    }
+    if (op.dreg == 0) {  // one factor for all of this thread's amplitudes
+      const cplx_t<T> f = M[cidx];
+#pragma unroll
+      for (int j = 0; j < (1 << R); ++j) v[j] = cmul<T>(v[j], f);
+      return;
+    }
+    if (op.dreg == 1) {
+      const cplx_t<T> f0 = M[cidx], f1 = M[cidx | (1u << op.dq)];
+      switch (op.dB) {
+        case 0: reg_diag1<T, R, 0>(v, f0, f1); break;
+        case 1: if constexpr (R > 1) reg_diag1<T, R, 1>(v, f0, f1); break;
+        case 2: if constexpr (R > 2) reg_diag1<T, R, 2>(v, f0, f1); break;
+        case 3: if constexpr (R > 3) reg_diag1<T, R, 3>(v, f0, f1); break;
+      }
+      return;
     }
     const uint4 jt = *reinterpret_cast<const uint4 *>(op.jidx);
     const uint32_t jw[4] = {jt.x, jt.y, jt.z, jt.w};
@@ -296,10 +337,10 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
   if (op.kind == 0 && op.swap) {
     // exactly X on a register bit (CNOT, Toffoli...): exchange registers
     switch (op.rb[0]) {
-      case 0: reg_swap<T, R, 0>(v, op.amask); break;
-      case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op.amask); break;
-      case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op.amask); break;
-      case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op.amask); break;
+      case 0: reg_swap<T, R, 0>(v, op); break;
+      case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op); break;
+      case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op); break;
+      case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op); break;
     }
     return;
   }
@@ -325,7 +366,7 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
+__global__ void __launch_bounds__(256, 3) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
                                                         const unsigned char *__restrict__ table, uint32_t nsubs,
                                                         uint32_t sops_off, uint32_t pool_off, uint32_t table_bytes,
                                                         uint32_t rho) {
@@ -355,6 +396,9 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
   const C *pool = reinterpret_cast<const C *>(tab + pool_off);
   const uint32_t row = threadIdx.x;
   const uint32_t mask = (1u << A.m) - 1;
+  constexpr uint32_t RHO = sizeof(T) == 4 ? 4u : 3u;  // the planner's bank-class bits (checked at launch)
+  // this thread's tile positions are (t + 256 i) << 1 (complex64) or t + 256 i
+  const uint32_t sw_t = sizeof(T) == 4 ? swz(threadIdx.x << 1, RHO) : swz(threadIdx.x, RHO);
   for (uint64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
     const uint64_t base = insert_zeros(t, A.lpos, int(A.L));
     // Issue every load of the tile before the first shared-memory store.
@@ -367,9 +411,9 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
       }
 #pragma unroll
       for (int i = 0; i < PER; ++i) {
-        const uint32_t p = (threadIdx.x + i * 256u) << 1;
-        tile[swz(p, rho)] = make_float2(x[i].x, x[i].y);
-        tile[swz(p + 1, rho)] = make_float2(x[i].z, x[i].w);
+        const uint32_t sp = sw_t ^ swz(512u * i, RHO);  // s(p), p = (t + 256 i) << 1; s(p + 1) = s(p) ^ 1
+        tile[sp] = make_float2(x[i].x, x[i].y);
+        tile[sp ^ 1u] = make_float2(x[i].z, x[i].w);
       }
     } else {
       C x[PER];
@@ -379,7 +423,7 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
         x[i] = __ldcs(psi + base + segoff[p >> A.m] + (p & mask));
       }
 #pragma unroll
-      for (int i = 0; i < PER; ++i) tile[swz(threadIdx.x + i * 256u, rho)] = x[i];
+      for (int i = 0; i < PER; ++i) tile[sw_t ^ swz(256u * i, RHO)] = x[i];
     }
     __syncthreads();
     for (uint32_t si = 0; si < nsubs; ++si) {
@@ -406,14 +450,15 @@ __global__ void __launch_bounds__(256) stage_reg_kernel(cplx_t<T> *__restrict__ 
 #pragma unroll
       for (int i = 0; i < PER; ++i) {
         const uint32_t p = (threadIdx.x + i * 256u) << 1;
-        const float2 a = tile[swz(p, rho)], b = tile[swz(p + 1, rho)];
+        const uint32_t sp = sw_t ^ swz(512u * i, RHO);
+        const float2 a = tile[sp], b = tile[sp ^ 1u];
         __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & mask)), make_float4(a.x, a.y, b.x, b.y));
       }
     } else {
 #pragma unroll
       for (int i = 0; i < PER; ++i) {
         const uint32_t p = threadIdx.x + i * 256u;
-        __stcs(psi + base + segoff[p >> A.m] + (p & mask), tile[swz(p, rho)]);
+        __stcs(psi + base + segoff[p >> A.m] + (p & mask), tile[sw_t ^ swz(256u * i, RHO)]);
       }
     }
     __syncthreads();
@@ -453,7 +498,8 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
   if (!plan.subs.empty()) {
     // Register substages: d_ops holds the table [SubstageDev...][SubOpDev...][pool].
     constexpr int R = sizeof(T) == 4 ? 4 : 3;
-    if (plan.r != unsigned(R) || plan.L != unsigned(R) + 8) return cudaErrorInvalidValue;
+    if (plan.r != unsigned(R) || plan.L != unsigned(R) + 8 || plan.rho != (sizeof(T) == 4 ? 4u : 3u))
+      return cudaErrorInvalidValue;
     const uint32_t sops_off = uint32_t(stage_subs_bytes(plan));
     const uint32_t pool_off = sops_off + uint32_t((plan.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16);
     const uint32_t table_bytes = pool_off + uint32_t((plan.pool.size() * sizeof(cplx_t<T>) + 15) / 16 * 16);

@@ -78,9 +78,11 @@ struct alignas(16) SubOpDev {
   uint8_t swap;     // dense 1-qubit: 1 if the matrix is exactly [[0, 1], [1, 0]]
   uint8_t cls;      // dense 1-qubit matrix class: 0 general, 1 real, 2 real diagonal with
                     // imaginary off-diagonal (Rx), 3 exact swap, 4 anti-diagonal
-  uint8_t pad;
+  uint8_t dreg;     // diagonal: number of its qubits that are register bits
   uint32_t amask;   // dense: register indices j that are group bases with the controls satisfied
-  uint32_t pad2[3];
+  uint8_t dq, dB;   // diagonal with dreg == 1: that qubit's index bit and register bit
+  uint8_t afull;    // dense: amask holds every group base (no controls among the register bits)
+  uint8_t pad[9];
 };
 static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
 static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with one 16-byte load");
@@ -248,6 +250,9 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
           } else if ((R >> op.tbit[q]) & 1) {
             so.dloc[q] = 0;
             so.didx[q] = uint8_t(reg_index(op.tbit[q]));
+            so.dreg++;
+            so.dq = uint8_t(q);
+            so.dB = so.didx[q];
           } else {
             so.dloc[q] = 1;
             so.didx[q] = uint8_t(row_index(op.tbit[q]));
@@ -271,8 +276,13 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
         }
         uint32_t tm = 0;
         for (unsigned q = 0; q < op.k; ++q) tm |= 1u << so.rb[q];
-        for (uint32_t x = 0; x < (1u << r); ++x)
-          if (!(x & tm) && (x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
+        uint32_t bases = 0;
+        for (uint32_t x = 0; x < (1u << r); ++x) {
+          if (x & tm) continue;
+          bases |= 1u << x;
+          if ((x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
+        }
+        so.afull = so.amask == bases ? 1 : 0;
       }
       sp.sops.push_back(so);
     }

@@ -12,6 +12,10 @@ using gsim::cplx;
 
 namespace {
 
+// set when a planned operation's metadata disagrees with itself; the entry
+// point then returns 1
+bool g_inconsistent = false;
+
 void apply_dense(std::vector<cplx> &psi, unsigned nq, const gsim::DenseOp &op) {
   const size_t k = op.pos.size(), d = size_t(1) << k;
   for (size_t i = 0; i < (size_t(1) << nq); ++i) {
@@ -111,19 +115,33 @@ void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::Stag
           if ((row & op.tctrl) != op.tctrl) continue;
           const cplx *M = sp.pool.data() + op.mat;
           if (op.kind == 2) {
+            // the kernel's three paths: one factor (no register qubit), two
+            // factors selected by register bit dB (one), a table (more)
+            uint32_t cidx = 0;
+            unsigned nreg = 0;
+            for (unsigned q = 0; q < op.dk; ++q) {
+              if (op.dloc[q] == 0) ++nreg;
+              else if (op.dloc[q] == 1) cidx |= ((row >> op.didx[q]) & 1u) << q;
+              else cidx |= uint32_t((base >> op.didx[q]) & 1) << q;
+            }
+            if (nreg != op.dreg) g_inconsistent = true;
             for (uint32_t j = 0; j < v.size(); ++j) {
-              uint32_t idx = 0;
-              for (unsigned q = 0; q < op.dk; ++q) {
-                uint32_t bit = op.dloc[q] == 0 ? (j >> op.didx[q]) & 1
-                               : op.dloc[q] == 1 ? (row >> op.didx[q]) & 1
-                                                 : uint32_t((base >> op.didx[q]) & 1);
-                idx |= bit << q;
+              uint32_t idx = cidx;
+              if (op.dreg == 1) {
+                idx |= ((j >> op.dB) & 1u) << op.dq;
+              } else if (op.dreg > 1) {
+                for (unsigned q = 0; q < op.dk; ++q)
+                  if (op.dloc[q] == 0) idx |= ((j >> op.didx[q]) & 1u) << q;
               }
               v[j] *= M[idx];
             }
           } else if (op.kind == 0) {
             // the kernel's 1-qubit paths: group bases from amask, one formula per class
             const unsigned B = op.rb[0];
+            uint32_t bases = 0;
+            for (uint32_t j = 0; j < v.size(); ++j)
+              if (!((j >> B) & 1)) bases |= 1u << j;
+            if ((op.afull != 0) != (op.amask == bases)) g_inconsistent = true;
             const cplx m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
             for (uint32_t j = 0; j < v.size(); ++j) {
               if ((j >> B) & 1) continue;
@@ -214,5 +232,7 @@ extern "C" int stage_plan_apply(unsigned nq, unsigned L, unsigned m, unsigned r,
     state[2 * i + 1] = psi[i].imag();
   }
   *nstages_out = ns;
-  return 0;
+  const bool bad = g_inconsistent;
+  g_inconsistent = false;
+  return bad ? 1 : 0;
 }

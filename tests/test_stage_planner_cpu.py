@@ -42,10 +42,10 @@ def plan_apply(lib, n, L, m, gates, psi, r=0, rho=4):
     st = np.ascontiguousarray(psi, dtype=np.complex128).copy()
     ns = C.c_uint32()
     P = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
-    lib.stage_plan_apply(C.c_uint(n), C.c_uint(L), C.c_uint(m), C.c_uint(r), C.c_uint(rho), C.c_size_t(len(gates)),
-                         P(ks, C.c_uint32),
-                         P(tg, C.c_uint32), P(cm, C.c_uint64), P(mats, C.c_double), P(st.view(np.float64), C.c_double),
-                         C.byref(ns))
+    rc = lib.stage_plan_apply(C.c_uint(n), C.c_uint(L), C.c_uint(m), C.c_uint(r), C.c_uint(rho),
+                              C.c_size_t(len(gates)), P(ks, C.c_uint32), P(tg, C.c_uint32), P(cm, C.c_uint64),
+                              P(mats, C.c_double), P(st.view(np.float64), C.c_double), C.byref(ns))
+    assert rc == 0, "planned operation metadata is inconsistent"
     return st, ns.value
 
 
