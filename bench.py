@@ -66,10 +66,11 @@ def parse():
                     help="profiling mode: time one precision only (no accuracy, e2e or CPU legs)")
     ap.add_argument("--init", choices=["random", "zero"], default="random",
                     help="initial state; kernel times do not depend on the amplitudes")
-    ap.add_argument("--workload", choices=["circuit", "fused", "adjoint", "learned"], default="circuit",
+    ap.add_argument("--workload", choices=["circuit", "fused", "adjoint", "learned", "gates"], default="circuit",
                     help="circuit: the 30-qubit headline; fused: k=5..7 dense gates at 32 qubits on tensor "
                          "cores; adjoint: energy + gradient of a 960-parameter ansatz at 24 qubits; learned: "
-                         "learned vs greedy fusion planning on random circuits")
+                         "learned vs greedy fusion planning on random circuits; gates: HBM bandwidth of the "
+                         "single-gate kernels (one pass per gate)")
     ap.add_argument("--ngates", type=int, default=60, help="fused workload: gates per step")
     return ap.parse_args()
 
@@ -122,6 +123,15 @@ class ClockSampler:
         reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(self.rows)}
+
+
+KERNEL_KINDS = ["dense_gate", "stage", "wide_gate", "tensor_core_gate"]
+# DRAM bytes (read + write) per amplitude of one stage-kernel launch, from the
+# ncu capture of the 26-qubit complex64 circuit (536.98 MB read + 482.32 MB
+# written per launch over 2^26 amplitudes); traffic grows with the state
+# size, so a 30-qubit launch moves 2^30 times this.
+NCU_TRAFFIC_PER_AMP = {(1, 1): (536.982016e6 + 482.322176e6) / 2 ** 26}
+NCU_TRAFFIC_SOURCE = "profiles/stage_reg_kernel_c64_26q_ncu.md, scaled from 2^26 to 2^nq amplitudes"
 
 
 def measured_peak():
@@ -334,6 +344,42 @@ def run_fused(a):
                       "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
 
 
+def run_gates(a):
+    """Single-gate kernels, one launch per gate (fusion "none"), on a 30-qubit
+    state: for each (precision, gate kind) the achieved HBM bandwidth
+    (algorithmic bytes / CUDA-event time per launch, mean over launches) as a
+    fraction of the measured copy bandwidth.  Targets cycle over every bit
+    position, so low (in-vector) and high (strided) targets are both timed."""
+    from projectq_gb300 import Simulator
+    from projectq_gb300.workloads import H, Rx, T, X
+
+    nq = a.qubits
+    peak, _ = measured_peak()
+    out = {}
+    cases = {
+        "1q_dense(H)": lambda q, n: (H, [q], []),
+        "1q_rx": lambda q, n: (Rx(0.3), [q], []),
+        "1q_diag(T)": lambda q, n: (T, [q], []),
+        "cnot": lambda q, n: (X, [q], [(q + 7) % n]),
+        "2q_dense": lambda q, n: (np.kron(Rx(0.2), H), [q, (q + 11) % n], []),
+        "3q_dense": lambda q, n: (np.kron(np.kron(Rx(0.2), H), Rx(0.5)), [q, (q + 11) % n, (q + 19) % n], []),
+    }
+    for prec in ("c64", "c128"):
+        sim = Simulator(1, precision=prec, fusion="none")
+        for q in range(nq):
+            sim.allocate_qubit(q)
+        for name, mk in cases.items():
+            gates = [mk(q, nq) for q in range(nq)]
+            ms, cnt, recs = timed_steps(sim, gates, max(1, a.steps), max(1, a.warmup), None)
+            gbs = [r["bytes"] / (r["ms"] * 1e-3) / 1e9 for r in recs if r["ms"] > 0]
+            mean = float(np.mean(gbs)) if gbs else 0.0
+            out[f"{prec}/{name}"] = {"launches": len(recs), "gbs_mean": round(mean, 1), "gbs_min": round(min(gbs), 1),
+                                     "frac_of_peak": round(mean / peak, 3)}
+        sim.close()
+    print(json.dumps({"workload": "single-gate kernels, one pass per gate", "qubits": nq, "peak_gbs": peak,
+                      "kernels": out}), flush=True)
+
+
 def run_adjoint(a):
     """Energy and gradient of the hardware-efficient ansatz (20 layers of Ry,
     Rz on each qubit + CNOT ladder: 960 parameters at 24 qubits) for a
@@ -406,7 +452,7 @@ def main():
         run_only(a)
         return
     if a.workload != "circuit":
-        {"fused": run_fused, "adjoint": run_adjoint, "learned": run_learned}[a.workload](a)
+        {"fused": run_fused, "adjoint": run_adjoint, "learned": run_learned, "gates": run_gates}[a.workload](a)
         return
     dist, world, rank, local = dist_init()
     from projectq_gb300 import Simulator
@@ -480,18 +526,28 @@ def main():
     if rank != 0:
         return
     peak, peak_src = measured_peak()
-    g = groups.get(key) if key else None
+    kern = {}
+    for r in recs:  # per kernel (kind, precision), all widths together
+        kg = kern.setdefault((r["kind"], r["precision"]), {"launches": 0, "ms": 0.0, "bytes": 0})
+        kg["launches"] += 1
+        kg["ms"] += r["ms"]
+        kg["bytes"] += r["bytes"]
     roofline = None
-    if g:
+    if kern:
+        kkey = max(kern, key=lambda k: kern[k]["ms"])
+        g = kern[kkey]
         avg_bytes = g["bytes"] / g["launches"]
         avg_ms = g["ms"] / g["launches"]
         achieved = avg_bytes / (avg_ms * 1e-3) / 1e9
+        per_amp = NCU_TRAFFIC_PER_AMP.get((kkey[0], kkey[1]))
         roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                    "frac": achieved / peak, "traffic": None, "peak_source": peak_src,
-                    "kernel": {"kind": ["dense_gate", "staged_tile"][key[0]], "k": key[1],
-                               "precision": "c64" if key[2] == 1 else "c128",
-                               "launches": g["launches"], "share": g["ms"] / max(1e-9, sum(x["ms"] for x in groups.values()))},
-                    "note": "achieved = algorithmic bytes per launch / mean per-launch CUDA-event time"}
+                    "frac": achieved / peak, "traffic": per_amp * 2 ** nq if per_amp else None,
+                    "traffic_source": NCU_TRAFFIC_SOURCE if per_amp else None, "peak_source": peak_src,
+                    "kernel": {"kind": KERNEL_KINDS[kkey[0]], "precision": "c64" if kkey[1] == 1 else "c128",
+                               "launches": g["launches"], "bytes_per_launch": avg_bytes, "ms_per_launch": avg_ms,
+                               "share": g["ms"] / max(1e-9, sum(x["ms"] for x in kern.values()))},
+                    "note": "achieved = algorithmic bytes per launch / mean per-launch CUDA-event time; the stage "
+                            "kernel applies ~30 gates per pass, so per gate it moves 30x these bytes"}
     value = world * G * a.steps / (ms64 * 1e-3)
     v128 = world * G * k128 / (ms128 * 1e-3)
     out = {

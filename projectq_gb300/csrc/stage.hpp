@@ -81,8 +81,7 @@ struct alignas(16) SubOpDev {
   uint8_t dreg;     // diagonal: number of its qubits that are register bits
   uint32_t amask;   // dense: register indices j that are group bases with the controls satisfied
   uint8_t dq, dB;   // diagonal with dreg == 1: that qubit's index bit and register bit
-  uint8_t afull;    // dense: amask holds every group base (no controls among the register bits)
-  uint8_t pad[9];
+  uint8_t pad[10];
 };
 static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
 static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with one 16-byte load");
@@ -276,13 +275,8 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
         }
         uint32_t tm = 0;
         for (unsigned q = 0; q < op.k; ++q) tm |= 1u << so.rb[q];
-        uint32_t bases = 0;
-        for (uint32_t x = 0; x < (1u << r); ++x) {
-          if (x & tm) continue;
-          bases |= 1u << x;
-          if ((x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
-        }
-        so.afull = so.amask == bases ? 1 : 0;
+        for (uint32_t x = 0; x < (1u << r); ++x)
+          if (!(x & tm) && (x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
       }
       sp.sops.push_back(so);
     }

@@ -138,10 +138,6 @@ void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::Stag
           } else if (op.kind == 0) {
             // the kernel's 1-qubit paths: group bases from amask, one formula per class
             const unsigned B = op.rb[0];
-            uint32_t bases = 0;
-            for (uint32_t j = 0; j < v.size(); ++j)
-              if (!((j >> B) & 1)) bases |= 1u << j;
-            if ((op.afull != 0) != (op.amask == bases)) g_inconsistent = true;
             const cplx m00 = M[0], m01 = M[1], m10 = M[2], m11 = M[3];
             for (uint32_t j = 0; j < v.size(); ++j) {
               if ((j >> B) & 1) continue;
