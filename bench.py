@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--per-layer", type=int, default=40)
     ap.add_argument("--fusion", default="staged", choices=["staged", "reference", "none"])
     ap.add_argument("--c128-steps", type=int, default=None, help="timed steps of the complex128 arm")
-    ap.add_argument("--e2e-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-gates", type=int, default=24, help="gates in the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--only", choices=["c64", "c128"], default=None,
@@ -127,10 +127,10 @@ class ClockSampler:
 
 KERNEL_KINDS = ["dense_gate", "stage", "wide_gate", "tensor_core_gate"]
 # DRAM bytes (read + write) per amplitude of one stage-kernel launch, from the
-# ncu capture of the 26-qubit complex64 circuit (536.98 MB read + 482.32 MB
+# ncu capture of the 26-qubit complex64 circuit (536.98 MB read + 478.86 MB
 # written per launch over 2^26 amplitudes); traffic grows with the state
 # size, so a 30-qubit launch moves 2^30 times this.
-NCU_TRAFFIC_PER_AMP = {(1, 1): (536.982016e6 + 482.322176e6) / 2 ** 26}
+NCU_TRAFFIC_PER_AMP = {(1, 1): (536.984576e6 + 478.860288e6) / 2 ** 26}
 NCU_TRAFFIC_SOURCE = "profiles/stage_reg_kernel_c64_26q_ncu.md, scaled from 2^26 to 2^nq amplitudes"
 
 
@@ -384,7 +384,9 @@ def run_adjoint(a):
     """Energy and gradient of the hardware-efficient ansatz (20 layers of Ry,
     Rz on each qubit + CNOT ladder: 960 parameters at 24 qubits) for a
     200-term random Pauli Hamiltonian, by one adjoint sweep; checked against
-    central finite differences (h = 1e-4) on 8 parameters."""
+    central finite differences (h = 1e-4) and the parameter-shift rule on 8
+    parameters; plus a batch of 16 parameter sets with 4, 8, 12 and 20
+    layers (complex64)."""
     from projectq_gb300 import Simulator
     from projectq_gb300.adjoint import energy_and_gradient, hardware_efficient_ansatz
     from projectq_gb300.workloads import random_pauli_hamiltonian
@@ -417,9 +419,30 @@ def run_adjoint(a):
                            - energy_and_gradient(sim, circ, tm, terms, range(nq))[0]) / (2 * h))
             fd = np.array(fd)
             rec["fd_max_rel_err"] = float(np.max(np.abs(g[idx] - fd)) / max(1.0, np.max(np.abs(fd))))
+            # parameter shift (exact for exp(-i theta P / 2)): (E(t + pi/2) - E(t - pi/2)) / 2
+            ps = []
+            for j in idx:
+                tp, tm = theta.copy(), theta.copy()
+                tp[j] += np.pi / 2
+                tm[j] -= np.pi / 2
+                ps.append((energy_and_gradient(sim, circ, tp, terms, range(nq))[0]
+                           - energy_and_gradient(sim, circ, tm, terms, range(nq))[0]) / 2)
+            rec["param_shift_max_abs_err"] = float(np.max(np.abs(g[idx] - np.array(ps))))
             g128 = g
         else:
             rec["max_abs_diff_vs_c128"] = float(np.max(np.abs(g - g128)))
+            # a batch of 16 parameter sets, 4 each of 4, 8, 12 and 20 layers
+            rng = np.random.default_rng(1)
+            batch = []
+            for layers in (4, 8, 12, 20):
+                c = hardware_efficient_ansatz(nq, layers)
+                for _ in range(4):
+                    batch.append((c, rng.uniform(-np.pi, np.pi, size=c.nparams)))
+            t0 = time.perf_counter()
+            for c, th in batch:
+                energy_and_gradient(sim, c, th, terms, range(nq))
+            rec["batch16_seconds"] = time.perf_counter() - t0
+            rec["batch16_parameters"] = int(sum(c.nparams for c, _ in batch))
         out[prec] = rec
     print(json.dumps(out), flush=True)
 
@@ -498,16 +521,21 @@ def main():
     e2e_times = []
     zz = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
     e2e_sim = s64
+    phases = []
     for i in range(a.e2e_steps + 1):
         e2e_sim.synchronize()
         t0 = time.perf_counter()
         e2e_sim.set_wavefunction(psi0, ids)
+        t1 = time.perf_counter()
         apply_circuit(e2e_sim, gates)
+        t2 = time.perf_counter()
         ev = e2e_sim.get_expectation_value(zz, ids)
         bits = e2e_sim.measure_qubits(ids)
-        dt = time.perf_counter() - t0
+        t3 = time.perf_counter()
+        dt = t3 - t0
         if i > 0:  # the first call pays one-time host page-locking costs
             e2e_times.append(dt)
+            phases.append((t1 - t0, t2 - t1, t3 - t2))
     pin.close()
     e2e = allreduce_max(dist, statistics.median(e2e_times))
 
@@ -546,8 +574,9 @@ def main():
                     "kernel": {"kind": KERNEL_KINDS[kkey[0]], "precision": "c64" if kkey[1] == 1 else "c128",
                                "launches": g["launches"], "bytes_per_launch": avg_bytes, "ms_per_launch": avg_ms,
                                "share": g["ms"] / max(1e-9, sum(x["ms"] for x in kern.values()))},
-                    "note": "achieved = algorithmic bytes per launch / mean per-launch CUDA-event time; the stage "
-                            "kernel applies ~30 gates per pass, so per gate it moves 30x these bytes"}
+                    "gates_per_launch": G * a.steps / max(1, g["launches"]),
+                    "note": "achieved = algorithmic bytes per launch / mean per-launch CUDA-event time; a stage "
+                            "launch applies gates_per_launch gates in one pass over the state"}
     value = world * G * a.steps / (ms64 * 1e-3)
     v128 = world * G * k128 / (ms128 * 1e-3)
     out = {
@@ -566,6 +595,8 @@ def main():
         "accuracy": {"one_minus_fidelity": one_minus_f, "max_abs_err": maxerr, "reference": "engine c128 path"},
         "e2e": {"value": world * G / e2e, "unit": "gates/s", "h2d_bytes_per_step": int(psi0.nbytes),
                 "d2h_bytes_per_step": 8 + nq, "seconds_per_step": e2e,
+                "phase_seconds_median": {k: statistics.median(p[j] for p in phases)
+                                         for j, k in enumerate(("upload", "submit_and_launch", "device_expectation_measure"))},
                 "path": "Simulator.set_wavefunction (pinned host c64) + apply_controlled_gate per gate + run "
                         "+ get_expectation_value + measure_qubits"},
         "gpu_launches": cnt64["gate_launches"],
