@@ -290,6 +290,9 @@ GSIM_API int gsim_launch_features(const gsim_launch_record *recs, size_t n, floa
 GSIM_API int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, const float *params);
 GSIM_API int gsim_set_learned_regimes(gsim_engine *e, const uint8_t *allowed, size_t count);
 GSIM_API int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms);
+/* The planner's own evaluation of the installed network (host FP32, the same
+ * arithmetic as gsim_mlp_predict's kernel) on n feature rows of 16. */
+GSIM_API int gsim_cost_model_predict(gsim_engine *e, const float *features, size_t n, float *out);
 
 /* The cost model's network: F inputs -> H -> H -> 1 (ReLU), FP32, with
  * hand-written forward, backward and Adam kernels (mlp.cu).  Parameters are

@@ -121,6 +121,7 @@ PRODUCT_ONLY = {
     "set_cost_model": (C.c_int, [_eng, C.c_int, C.c_int, C.POINTER(C.c_float)]),
     "set_learned_regimes": (C.c_int, [_eng, _u8p, _sz]),
     "last_plan_choice": (C.c_int, [_eng, C.POINTER(C.c_int), _f64p]),
+    "cost_model_predict": (C.c_int, [_eng, C.POINTER(C.c_float), _sz, C.POINTER(C.c_float)]),
     "mlp_create": (C.c_int, [C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_void_p)]),
     "mlp_destroy": (C.c_int, [C.c_void_p]),
     "mlp_num_params": (C.c_int, [C.c_void_p, C.POINTER(_sz)]),

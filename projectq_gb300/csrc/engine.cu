@@ -644,6 +644,10 @@ class Engine {
   }
   int last_choice() const { return last_choice_; }
   void last_prediction(double *out) const { std::copy(last_pred_, last_pred_ + 3, out); }
+  void predict_rows(const float *x, size_t n, float *out) const {
+    if (cm_.empty()) fail(GSIM_ERR_VALUE, "no cost model installed");
+    for (size_t i = 0; i < n; ++i) out[i] = predict(x + i * kFeatures);
+  }
 
   void set_fusion(int mode, unsigned kmax) {
     run();
@@ -779,14 +783,15 @@ class Engine {
     const int route = dense_kind(kq);
     if (route == 3) {
       // tensor cores: U embedded as a real 2^(k+1) square matrix, TF32 hi/lo
+      const DenseOp sop = tc_sorted_targets(op);
       const size_t nb = tc_operand_floats(int(kq)) * 4;
       char *h = nullptr;
       UploadSlot &sl = next_slot(nb, h);
-      tc_prepare_operand(op.m, int(kq), reinterpret_cast<float *>(h));
+      tc_prepare_operand(sop.m, int(kq), reinterpret_cast<float *>(h));
       const void *d = finish_slot(sl, h, nb);
       int *d_err = reinterpret_cast<int *>(static_cast<char *>(small_.get(4096)) + 2048);
       if (!tc_used_) CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
-      CK(launch_tc_gate(state_.p, N_, op, static_cast<const float *>(d), d_err, stream_));
+      CK(launch_tc_gate(state_.p, N_, sop, static_cast<const float *>(d), d_err, stream_));
       tc_used_ = true;
     } else if (route == 2) {
       const size_t D = size_t(1) << op.pos.size();
@@ -1918,6 +1923,9 @@ int gsim_set_learned_regimes(gsim_engine *e, const uint8_t *allowed, size_t coun
     if (count > 65) fail(GSIM_ERR_LENGTH, "set_learned_regimes(): at most 65 entries");
     E(e)->set_learned_regimes(allowed, count);
   });
+}
+int gsim_cost_model_predict(gsim_engine *e, const float *features, size_t n, float *out) {
+  return guard([&] { E(e)->predict_rows(features, n, out); });
 }
 int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms) {
   return guard([&] {

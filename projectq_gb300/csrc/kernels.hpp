@@ -19,6 +19,9 @@ cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cu
 // lo parts, laid out by tc_prepare_operand (tc_operand_floats(k) floats);
 // *d_err is set when a wait inside the kernel times out.
 size_t tc_operand_floats(int k);
+// The gate with its targets sorted ascending (matrix permuted to match): the
+// kernel loads and stores adjacent amplitude pairs when a target is bit 0.
+DenseOp tc_sorted_targets(const DenseOp &op);
 void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out);
 cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s);
 // Gates of up to 7 targets; d_matrix: the 2^k x 2^k matrix (row-major) in the

@@ -183,30 +183,46 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
       : "memory");
 }
 
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 64 consecutive accumulator columns of this warp's 32 TMEM lanes (one
+// register per column), with the wait for the load inside the same asm so the
+// values are only used after they have arrived.
+__device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
+  uint32_t r[64];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      "tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32,%33,%34,%35,%36,%37,%38,%39,%40,%41,%42,%43,%44,%45,%46,%47,%48,%49,%50,%51,%52,%53,%54,%55,%56,%57,%58,%59,%60,%61,%62,%63}, [%64];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+      : "r"(taddr)
+      : "memory");
 #pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
 }
 
 __device__ __forceinline__ uint64_t group_base(const TcArgs &A, uint64_t g) {
   return insert_zeros(g, A.ins, A.nins) | A.ctrl_set;
 }
 
-// Producer: one K-chunk (8 amplitudes of one group) into registers.
-template <int KQ>
+// Producer: one K-chunk (8 amplitudes of one group) into registers.  PAIR:
+// the first target is bit 0, so amplitudes j and j + 1 (j even) are adjacent
+// and 16-byte aligned in the state: one 16-byte load per pair.
+template <bool PAIR>
 __device__ __forceinline__ void gather8(const float2 *__restrict__ psi, const TcArgs &A, uint64_t base, bool active,
                                         int ch, int half, float2 (&x)[8]) {
+  if constexpr (PAIR) {
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int j = ch * kAmpsPerChunk + half * 8 + q;
-    x[q] = active ? psi[base + A.off[j]] : make_float2(0.f, 0.f);
+    for (int q = 0; q < 8; q += 2) {
+      const int j = ch * kAmpsPerChunk + half * 8 + q;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (active) v = *reinterpret_cast<const float4 *>(psi + base + A.off[j]);
+      x[q] = make_float2(v.x, v.y);
+      x[q + 1] = make_float2(v.z, v.w);
+    }
+  } else {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int j = ch * kAmpsPerChunk + half * 8 + q;
+      x[q] = active ? psi[base + A.off[j]] : make_float2(0.f, 0.f);
+    }
   }
 }
 
@@ -231,7 +247,7 @@ __device__ __forceinline__ void split_store(unsigned char *st, int row, int half
   }
 }
 
-template <int KQ>
+template <int KQ, bool PAIR>
 __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
     tc_gate_kernel(float2 *__restrict__ psi, const float *__restrict__ bsrc, const __grid_constant__ TcArgs A,
                    int *err) {
@@ -298,7 +314,7 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
     }
     auto load_next = [&](float2 (&x)[8]) {
       if (loaded >= total) return;
-      gather8<KQ>(psi, A, lbase, lact, lc, half, x);
+      gather8<PAIR>(psi, A, lbase, lact, lc, half, x);
       ++loaded;
       if (++lc == NCH) {
         lc = 0;
@@ -348,13 +364,21 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       const uint64_t g = tile * kRows + uint64_t(row);
       const bool active = g < A.groups;
       const uint64_t base = active ? group_base(A, g) : 0;
+      // 64 columns (32 outputs) per TMEM load: one wait per 64 columns
 #pragma unroll 1
-      for (int c0 = 0; c0 < N; c0 += 16) {
-        float v[16];
-        tmem_ld16(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+      for (int c0 = 0; c0 < N; c0 += 64) {
+        float v[64];
+        tmem_ld64(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
         if (active) {
+          if constexpr (PAIR) {
 #pragma unroll
-          for (int q = 0; q < 8; ++q) __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
+            for (int q = 0; q < 32; q += 2)
+              __stcs(reinterpret_cast<float4 *>(psi + base + A.off[c0 / 2 + q]),
+                     make_float4(v[2 * q], v[2 * q + 1], v[2 * q + 2], v[2 * q + 3]));
+          } else {
+#pragma unroll
+            for (int q = 0; q < 32; ++q) __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
+          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -447,8 +471,8 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
                  : "memory");
 }
 
-template <int KQ>
-cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
+template <int KQ, bool PAIR>
+cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
   using Cfg = TcCfg<KQ>;
   TcArgs A;
   std::memset(&A, 0, sizeof(A));
@@ -467,7 +491,7 @@ cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *
   A.groups = uint64_t(1) << (nq - ins.size());
   static bool attr = false;
   if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gate_kernel<KQ>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(tc_gate_kernel<KQ, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          int(Cfg::kSmem));
     if (e != cudaSuccess) return e;
     attr = true;
@@ -477,11 +501,38 @@ cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const uint64_t ntiles = (A.groups + kRows - 1) / kRows;
   const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(sms))));
-  tc_gate_kernel<KQ><<<grid, Cfg::kThreads, Cfg::kSmem, s>>>(static_cast<float2 *>(psi), d_b, A, d_err);
+  tc_gate_kernel<KQ, PAIR><<<grid, Cfg::kThreads, Cfg::kSmem, s>>>(static_cast<float2 *>(psi), d_b, A, d_err);
   return cudaGetLastError();
 }
 
+template <int KQ>
+cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
+  if (op.pos[0] == 0) return launch_tc_kp<KQ, true>(psi, nq, op, d_b, d_err, s);
+  return launch_tc_kp<KQ, false>(psi, nq, op, d_b, d_err, s);
+}
+
 }  // namespace
+
+// The same gate with its targets in ascending bit order (rows and columns of
+// the matrix permuted to match), so that a target at bit 0 is matrix bit 0.
+DenseOp tc_sorted_targets(const DenseOp &op) {
+  const size_t k = op.pos.size(), D = size_t(1) << k;
+  std::vector<unsigned> perm(k);
+  for (size_t l = 0; l < k; ++l) perm[l] = unsigned(l);
+  std::sort(perm.begin(), perm.end(), [&](unsigned a, unsigned b) { return op.pos[a] < op.pos[b]; });
+  DenseOp out;
+  out.ctrl_mask = op.ctrl_mask;
+  out.pos.resize(k);
+  for (size_t l = 0; l < k; ++l) out.pos[l] = op.pos[perm[l]];
+  std::vector<size_t> old(D, 0);  // new index -> old index
+  for (size_t j = 0; j < D; ++j)
+    for (size_t l = 0; l < k; ++l)
+      if ((j >> l) & 1) old[j] |= size_t(1) << perm[l];
+  out.m.resize(D * D);
+  for (size_t a = 0; a < D; ++a)
+    for (size_t j = 0; j < D; ++j) out.m[a * D + j] = op.m[old[a] * D + old[j]];
+  return out;
+}
 
 size_t tc_operand_floats(int k) { return size_t(2) * size_t(2 << k) * size_t(2 << k); }
 

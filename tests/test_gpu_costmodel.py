@@ -59,6 +59,21 @@ def test_forward_and_gradient_match_numpy():
     assert np.max(np.abs(g - gr)) <= 1e-4 * max(1.0, np.max(np.abs(gr)))
 
 
+def test_planner_evaluates_the_network_like_the_kernel():
+    """The planner's host forward pass equals the CUDA inference kernel's."""
+    rng = np.random.default_rng(7)
+    net = cm.MLP(seed=9)
+    X = rng.uniform(0, 1, size=(300, cm.F)).astype(np.float32)
+    s = make("gpu", seed=1, precision="c64", fusion="staged")
+    allocate(s, 4)
+    cm.install(s, net.params, regimes=np.ones(65, np.uint8))
+    host = np.zeros(len(X), dtype=np.float32)
+    s._check(s._api.cost_model_predict(s._h, X.ctypes.data_as(cm.C.POINTER(cm.C.c_float)), len(X),
+                                       host.ctypes.data_as(cm.C.POINTER(cm.C.c_float))))
+    dev = net.predict(X)
+    assert np.max(np.abs(host - dev)) <= 1e-5 * max(1.0, float(np.max(np.abs(dev))))
+
+
 def test_training_fits_a_smooth_target():
     rng = np.random.default_rng(1)
     X = rng.uniform(-1, 1, size=(512, cm.F)).astype(np.float32)
