@@ -101,6 +101,16 @@ GSIM_API int gsim_measure_qubits(gsim_engine *e, const uint32_t *ids, size_t n, 
 GSIM_API int gsim_measure_qubits_at(gsim_engine *e, const uint32_t *ids, size_t n, double rnd,
                            uint8_t *out);
 
+/* A stream of n gates in one call, the same as n gsim_apply_controlled_gate
+ * calls in order (no reference counterpart: the reference's Python layer calls
+ * apply_controlled_gate per gate, _simulator.py:404-415).  Gate g has nt[g]
+ * targets and nc[g] controls; `qubits` holds, gate after gate, its targets
+ * then its controls; `mats` holds, gate after gate, its 2^nt x 2^nt matrix
+ * (row-major, interleaved re/im).  On an error, the gates before the failing
+ * one have been queued and *failed_at (if not NULL) is its index. */
+GSIM_API int gsim_apply_gates(gsim_engine *e, size_t n, const uint32_t *nt, const uint32_t *nc,
+                              const uint32_t *qubits, const double *mats, size_t *failed_at);
+
 /* apply_controlled_gate — simulator.hpp:204-222 (fusion: fusion.hpp:56-63). */
 GSIM_API int gsim_apply_controlled_gate(gsim_engine *e, const double *m, uint32_t k,
                                const uint32_t *ids, const uint32_t *ctrl, size_t nctrl);

@@ -1700,6 +1700,25 @@ int gsim_apply_controlled_gate(gsim_engine *e, const double *m, uint32_t k, cons
     E(e)->apply_controlled_gate(std::move(M), vu(ids, k), vu(ctrl, nctrl));
   });
 }
+int gsim_apply_gates(gsim_engine *e, size_t n, const uint32_t *nt, const uint32_t *nc, const uint32_t *qubits,
+                     const double *mats, size_t *failed_at) {
+  size_t g = 0;
+  const int rc = guard([&] {
+    size_t qo = 0, mo = 0;
+    for (; g < n; ++g) {
+      const uint32_t k = nt[g];
+      if (k == 0 || k > 16) gsim::fail(GSIM_ERR_VALUE, "apply_gates(): bad gate width");
+      const size_t d = size_t(1) << k;
+      std::vector<gsim::cplx> M(d * d);
+      for (size_t i = 0; i < d * d; ++i) M[i] = gsim::cplx(mats[mo + 2 * i], mats[mo + 2 * i + 1]);
+      E(e)->apply_controlled_gate(std::move(M), vu(qubits + qo, k), vu(qubits + qo + k, nc[g]));
+      qo += k + nc[g];
+      mo += 2 * d * d;
+    }
+  });
+  if (failed_at) *failed_at = rc == GSIM_OK ? n : g;
+  return rc;
+}
 int gsim_run(gsim_engine *e) {
   return guard([&] { E(e)->run(); });
 }

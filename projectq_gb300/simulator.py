@@ -383,11 +383,30 @@ class Simulator:
         self._check(self._api.reset_counters(self._h))
 
     def apply_gates(self, gates):
-        """Submit many gates in one call: [(matrix, target ids, control ids), ...]
-        (the same gates apply_controlled_gate takes, without per-gate ctypes
-        round trips for the matrix conversion)."""
-        for m, t, c in gates:
-            self.apply_controlled_gate(m, t, c)
+        """Submit many gates in one call: [(matrix, target ids, control ids), ...],
+        the same as apply_controlled_gate per gate, packed into flat arrays and
+        queued by one gsim_apply_gates call (no per-gate ctypes round trip)."""
+        gates = list(gates)
+        if not gates:
+            return
+        nt = np.empty(len(gates), dtype=np.uint32)
+        nc = np.empty(len(gates), dtype=np.uint32)
+        qubits, mats = [], []
+        for g, (m, t, c) in enumerate(gates):
+            t, c = _ids(t), _ids(c)
+            mat = np.asarray(m, dtype=np.complex128)
+            if mat.ndim != 2 or mat.shape != (1 << len(t), 1 << len(t)):
+                raise ValueError(f"apply_gates(): gate {g}: a {len(t)}-qubit gate needs a "
+                                 f"{1 << len(t)}x{1 << len(t)} matrix")
+            nt[g], nc[g] = len(t), len(c)
+            qubits.extend(t)
+            qubits.extend(c)
+            mats.append(mat.reshape(-1))
+        qa = _u32(qubits)
+        ma = np.ascontiguousarray(np.concatenate(mats)).view(np.float64)
+        failed = C.c_size_t()
+        self._check(self._api.apply_gates(self._h, len(gates), _p(nt, C.c_uint32), _p(nc, C.c_uint32),
+                                          _p(qa, C.c_uint32), _p(ma, C.c_double), C.byref(failed)))
 
     def cuda_array(self):
         """Zero-copy view of the flushed device state: an object with

@@ -315,3 +315,25 @@ def test_errors_match_reference_types():
     g.run()
     with pytest.raises(RuntimeError):
         g.deallocate_qubit(0)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("fusion", ["reference", "staged"])
+def test_gate_stream_equals_per_gate_calls(prec, fusion):
+    """gsim_apply_gates (one call for many gates) queues exactly what the same
+    apply_controlled_gate calls queue; a malformed gate in the stream raises
+    and the gates before it stay queued."""
+    n = 10
+    gates = random_mixed_circuit(n, 80, 7, kmax=4, max_ctrl=2)
+    g, o = pair(n, prec, fusion=fusion)
+    g.apply_gates(gates)
+    g.run()
+    run_circuit(o, gates)
+    assert_states(g, o, prec)
+    g2, o2 = pair(n, prec, fusion=fusion)
+    bad = gates[:5] + [(np.eye(4), [0, 0], [])] + gates[5:]
+    with pytest.raises(ValueError):
+        g2.apply_gates(bad)
+    g2.run()
+    run_circuit(o2, gates[:5])
+    assert_states(g2, o2, prec)
