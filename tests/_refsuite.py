@@ -20,14 +20,19 @@ def available():
     return all((REF_PY / m).exists() for m in MODULES)
 
 
-def run(backend, precision="c128", fusion="reference", extra=()):
+UNITARY_MODULE = "projectq/backends/_unitary_test.py"
+
+
+def run(backend, precision="c128", fusion="reference", extra=(), unitary=False):
     env = dict(os.environ)
     env["PYTHONPATH"] = os.pathsep.join([str(HERE / "_stubs"), str(REF_PY), str(HERE), str(ROOT),
                                          env.get("PYTHONPATH", "")])
-    env.update(GSIM_BACKEND=backend, GSIM_PRECISION=precision, GSIM_FUSION=fusion)
+    env.update(GSIM_BACKEND=backend, GSIM_PRECISION=precision, GSIM_FUSION=fusion,
+               GSIM_UNITARY="1" if unitary else "0")
+    modules = [UNITARY_MODULE] if unitary else MODULES
     cmd = [sys.executable, "-m", "pytest", "-q", "-p", "ref_suite_plugin", "-p", "no:cacheprovider",
-           "--rootdir", str(REF_PY), *[str(REF_PY / m) for m in MODULES]]
-    for d in DESELECT:
+           "--rootdir", str(REF_PY), *[str(REF_PY / m) for m in modules]]
+    for d in ([] if unitary else DESELECT):
         cmd += ["--deselect", str(REF_PY / d)]
     cmd += list(extra)
     res = subprocess.run(cmd, cwd=str(REF_PY), env=env, capture_output=True, text=True, timeout=1800)

@@ -9,6 +9,8 @@ Environment:
   GSIM_BACKEND    "gpu" (default; libgb300sim.so) or "oracle" (CPU restatement)
   GSIM_PRECISION  "c128" (default) or "c64"
   GSIM_FUSION     "reference" (default), "none" or "staged"
+  GSIM_UNITARY    "1": also serve projectq.backends.UnitarySimulator
+                  (backends/_unitary.py) from projectq_gb300.unitary
 """
 
 import os
@@ -22,9 +24,9 @@ def pytest_configure(config):
     fusion = os.environ.get("GSIM_FUSION", "reference")
     from projectq_gb300 import Simulator
 
-    if backend == "oracle":
-        from _backends import oracle_api
+    from _backends import oracle_api
 
+    if backend == "oracle":
         api = oracle_api()
 
         def factory(seed=1, *args):
@@ -41,3 +43,16 @@ def pytest_configure(config):
     import projectq.backends._sim as pkg
 
     pkg._cppsim = mod
+    if os.environ.get("GSIM_UNITARY") == "1":
+        import projectq.backends as backends
+        import projectq.backends._unitary as umod
+        from projectq_gb300.unitary import UnitarySimulator
+
+        uapi = oracle_api() if backend == "oracle" else None
+
+        class ServedUnitarySimulator(UnitarySimulator):
+            def __init__(self):
+                super().__init__(precision=prec, _api=uapi)
+
+        umod.UnitarySimulator = ServedUnitarySimulator
+        backends.UnitarySimulator = ServedUnitarySimulator

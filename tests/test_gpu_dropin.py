@@ -41,6 +41,58 @@ def test_reference_suite_complex64():
     assert passed >= 50
 
 
+def test_reference_unitary_suite():
+    """ProjectQ's UnitarySimulator tests (backends/_unitary_test.py) with
+    projectq_gb300.unitary.UnitarySimulator (vec(U) on the GPU) in its place."""
+    rc, passed, out = _refsuite.run("gpu", "c128", unitary=True)
+    assert rc == 0, out[-6000:]
+    assert passed >= 8
+
+
+def test_unitary_matches_reference_class_on_random_circuits():
+    """The GPU UnitarySimulator against ProjectQ's own (dense NumPy) class on
+    random controlled circuits over 6 qubits (1e-12)."""
+    if not projectq_available():
+        pytest.skip("ProjectQ not importable")
+    from projectq import MainEngine
+    from projectq.backends import UnitarySimulator as RefUnitary
+    from projectq.meta import Control
+    from projectq.ops import CNOT, H, Rx, Ry, Rz, T, Toffoli
+
+    from projectq_gb300.unitary import UnitarySimulator
+
+    def build(backend, seed):
+        rng = np.random.default_rng(seed)
+        eng = MainEngine(backend=backend, engine_list=[])
+        qureg = eng.allocate_qureg(6)
+        for _ in range(60):
+            kind = int(rng.integers(6))
+            a, b, c = (int(v) for v in rng.choice(6, 3, replace=False))
+            th = float(rng.uniform(0, 2 * np.pi))
+            if kind == 0:
+                H | qureg[a]
+            elif kind == 1:
+                Rx(th) | qureg[a]
+            elif kind == 2:
+                CNOT | (qureg[a], qureg[b])
+            elif kind == 3:
+                Toffoli | (qureg[a], qureg[b], qureg[c])
+            elif kind == 4:
+                with Control(eng, qureg[b]):
+                    Ry(th) | qureg[a]
+            else:
+                T | qureg[a]
+                Rz(th) | qureg[b]
+        eng.flush()
+        return eng, qureg
+
+    for seed in (0, 1):
+        ours, ref = UnitarySimulator(), RefUnitary()
+        build(ours, seed)
+        build(ref, seed)
+        assert np.max(np.abs(ours.unitary - ref.unitary)) < 1e-12
+
+
 def test_time_evolution_against_scipy_expm():
     """The reference's time-evolution check (_simulator_test.py:514-570) with
     NumPy-2-safe array conversion: controlled exp(-i t H) on 8 qubits vs
