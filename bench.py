@@ -292,6 +292,43 @@ def run_only(a):
                       "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
 
 
+def sampled_group_check(sim, nq, haar_unitary, rng, k=7, ngroups=16):
+    """Apply H to every qubit (so no amplitude is zero), then one Haar k-qubit
+    gate with a target below 5; read 16 random amplitude groups before and
+    after it and compare with the FP64 product U x on the host."""
+    from projectq_gb300.workloads import H
+
+    for q in range(nq):
+        sim.apply_controlled_gate(H, [q], [])
+    sim.run()
+    low = int(rng.integers(0, 5))
+    rest = [int(q) for q in rng.permutation(nq) if q != low]
+    targets = [low] + rest[: k - 1]
+    U = haar_unitary(k, rng)
+    ids = list(range(nq))
+
+    def amp(index):
+        return sim.get_amplitude([(index >> q) & 1 for q in range(nq)], ids)
+
+    offs = [sum(((j >> l) & 1) << targets[l] for l in range(k)) for j in range(1 << k)]
+    tmask = sum(1 << t for t in targets)
+    bases = []
+    while len(bases) < ngroups:
+        b = int(rng.integers(0, 1 << nq)) & ~tmask
+        if b not in bases:
+            bases.append(b)
+    xs = [np.array([amp(b + o) for o in offs], dtype=np.complex128) for b in bases]
+    sim.apply_controlled_gate(U, targets, [])
+    sim.run()
+    err, scale = 0.0, 0.0
+    for b, x in zip(bases, xs):
+        y = np.array([amp(b + o) for o in offs], dtype=np.complex128)
+        ref = U @ x
+        err = max(err, float(np.max(np.abs(y - ref))))
+        scale = max(scale, float(np.max(np.abs(ref))))
+    return {"qubits": nq, "k": k, "groups": ngroups, "max_abs_err": err, "max_abs_err_relative": err / scale}
+
+
 def run_fused(a):
     """Dense Haar-random k-qubit gates, k uniform in {5, 6, 7}, on a 32-qubit
     complex64 state (32 GiB); targets always include a qubit below 5 and one
@@ -336,11 +373,17 @@ def run_fused(a):
     ip, maxerr = res["c128"].compare(res["c64"])
     n1 = res["c128"].compare(res["c128"])[0].real
     n2 = res["c64"].compare(res["c64"])[0].real
+    for s_ in res.values():
+        s_.close()
+    # sampled check at full width: one more k = 7 gate on the spread-out state,
+    # 16 random groups read before and after and compared with an FP64 product
+    sampled = sampled_group_check(sim, nq, haar_unitary, np.random.default_rng(5))
     print(json.dumps({"workload": "fused k=5..7 dense gates", "qubits": nq, "gates_per_step": len(gates),
                       "ms_per_step": ms / a.steps, "gates_per_s": len(gates) * a.steps / (ms * 1e-3),
                       "algorithmic_tflops": flops / (ms * 1e-3) / 1e12,
                       "hbm_gbs": cnt["gate_bytes"] / (ms * 1e-3) / 1e9,
                       "accuracy_24q_30gates": {"one_minus_fidelity": 1 - abs(ip) ** 2 / (n1 * n2), "max_abs_err": maxerr},
+                      "accuracy_sampled_full_width": sampled,
                       "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
 
 
