@@ -980,7 +980,7 @@ class Engine {
   unsigned fmin_ = 4, fmax_ = 5, max_gate_ = 5;
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
-  unsigned tile_bits_c64_ = 12, tile_bits_c128_ = 11;
+  unsigned tile_bits_c64_ = kRegBitsC64 + 8, tile_bits_c128_ = kRegBitsC128 + 8;
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
   bool tc_used_ = false;
@@ -1114,14 +1114,14 @@ uint64_t Engine::sample(double rnd) {
 }
 
 std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) const {
-  // Tiles of 32 KB: 2^12 complex64 or 2^11 complex128 amplitudes, with runs
-  // of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
+  // Tiles of 2^(r + 8) amplitudes (64 KB complex64, 32 KB complex128), with
+  // runs of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
   const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
   const unsigned m = prec_ == GSIM_C64 ? 5 : 4;
   StagePlanner planner(N_, L, m);
   std::vector<PlanStep> steps = planner.plan(gates);
   // Register substages where the tile is 2^(r + 8) amplitudes (256 threads).
-  const unsigned r = prec_ == GSIM_C64 ? 4 : 3, rho = prec_ == GSIM_C64 ? 4 : 3;
+  const unsigned r = prec_ == GSIM_C64 ? kRegBitsC64 : kRegBitsC128, rho = prec_ == GSIM_C64 ? 4 : 3;
   for (auto &st : steps)
     if (st.is_stage && use_reg_stages_ && st.stage.L == r + 8) build_substages(st.stage, r, rho);
   return steps;

@@ -307,11 +307,14 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
         case 1: if constexpr (R > 1) reg_diag1<T, R, 1>(v, f0, f1); break;
         case 2: if constexpr (R > 2) reg_diag1<T, R, 2>(v, f0, f1); break;
         case 3: if constexpr (R > 3) reg_diag1<T, R, 3>(v, f0, f1); break;
+        case 4: if constexpr (R > 4) reg_diag1<T, R, 4>(v, f0, f1); break;
       }
       return;
     }
     const uint4 jt = *reinterpret_cast<const uint4 *>(op.jidx);
-    const uint32_t jw[4] = {jt.x, jt.y, jt.z, jt.w};
+    uint4 jt2 = make_uint4(0, 0, 0, 0);
+    if constexpr (R > 4) jt2 = *reinterpret_cast<const uint4 *>(op.jidx + 16);
+    const uint32_t jw[8] = {jt.x, jt.y, jt.z, jt.w, jt2.x, jt2.y, jt2.z, jt2.w};
 #pragma unroll
     for (int j = 0; j < (1 << R); ++j) {
       const uint32_t idx = cidx | ((jw[j >> 2] >> (8 * (j & 3))) & 0xFFu);
@@ -326,6 +329,7 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
       case 1: if constexpr (R > 1) reg_swap<T, R, 1>(v, op); break;
       case 2: if constexpr (R > 2) reg_swap<T, R, 2>(v, op); break;
       case 3: if constexpr (R > 3) reg_swap<T, R, 3>(v, op); break;
+      case 4: if constexpr (R > 4) reg_swap<T, R, 4>(v, op); break;
     }
     return;
   }
@@ -335,23 +339,26 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
       case 1: if constexpr (R > 1) reg_dense1_cls<T, R, 1>(v, op, M); break;
       case 2: if constexpr (R > 2) reg_dense1_cls<T, R, 2>(v, op, M); break;
       case 3: if constexpr (R > 3) reg_dense1_cls<T, R, 3>(v, op, M); break;
+      case 4: if constexpr (R > 4) reg_dense1_cls<T, R, 4>(v, op, M); break;
     }
     return;
   }
-  const int key = op.rb[0] * 4 + op.rb[1];
+  const int key = op.rb[0] * 8 + op.rb[1];
 #define GSIM_D2(a, b) \
-  case a * 4 + b:     \
+  case a * 8 + b:     \
     if constexpr (R > a && R > b) reg_dense2<T, R, a, b>(v, op, M); \
     break;
   switch (key) {
     GSIM_D2(0, 1) GSIM_D2(1, 0) GSIM_D2(0, 2) GSIM_D2(2, 0) GSIM_D2(0, 3) GSIM_D2(3, 0)
     GSIM_D2(1, 2) GSIM_D2(2, 1) GSIM_D2(1, 3) GSIM_D2(3, 1) GSIM_D2(2, 3) GSIM_D2(3, 2)
+    GSIM_D2(0, 4) GSIM_D2(4, 0) GSIM_D2(1, 4) GSIM_D2(4, 1) GSIM_D2(2, 4) GSIM_D2(4, 2)
+    GSIM_D2(3, 4) GSIM_D2(4, 3)
   }
 #undef GSIM_D2
 }
 
 template <typename T, int R>
-__global__ void __launch_bounds__(256, 3) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
+__global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
                                                         const unsigned char *__restrict__ table, uint32_t nsubs,
                                                         uint32_t sops_off, uint32_t pool_off, uint32_t table_bytes,
                                                         uint32_t rho) {
@@ -482,7 +489,7 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
   }
   if (!plan.subs.empty()) {
     // Register substages: d_ops holds the table [SubstageDev...][SubOpDev...][pool].
-    constexpr int R = sizeof(T) == 4 ? 4 : 3;
+    constexpr int R = sizeof(T) == 4 ? int(kRegBitsC64) : int(kRegBitsC128);
     if (plan.r != unsigned(R) || plan.L != unsigned(R) + 8 || plan.rho != (sizeof(T) == 4 ? 4u : 3u))
       return cudaErrorInvalidValue;
     const uint32_t sops_off = uint32_t(stage_subs_bytes(plan));

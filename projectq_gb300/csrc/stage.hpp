@@ -31,6 +31,7 @@
 #include <cstdint>
 #include <cstddef>
 #include <cstring>
+#include <stdexcept>
 #include <vector>
 
 #include "ops.hpp"
@@ -63,8 +64,12 @@ struct StageOpDev {
 // swizzled order s(p) = p ^ fold(p >> rho), fold XOR-ing rho-bit chunks, so
 // tile bit b lands in bank class b mod rho; the five lane bits are chosen to
 // cover every class, which makes each register access conflict-free.
+// Register bits per thread of the register-substage kernel (tile = 2^(r + 8)
+// amplitudes, 256 threads): 32 complex64 / 8 complex128 amplitudes per thread.
+constexpr unsigned kRegBitsC64 = 5, kRegBitsC128 = 3, kMaxRegBits = 5;
+
 struct alignas(16) SubOpDev {
-  uint8_t jidx[16]; // diagonal: index bits contributed by the register qubits, per j (16-byte aligned)
+  uint8_t jidx[32]; // diagonal: index bits contributed by the register qubits, per j (16-byte aligned)
   uint64_t gctrl;   // non-local controls (global mask)
   uint32_t kind;    // 0 dense 1-qubit, 1 dense 2-qubit, 2 diagonal
   uint32_t mat;     // offset in the stage's pool
@@ -84,10 +89,10 @@ struct alignas(16) SubOpDev {
   uint8_t pad[10];
 };
 static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
-static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with one 16-byte load");
+static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with 16-byte loads");
 struct SubstageDev {
   uint32_t op_begin, op_end;
-  uint32_t soff[16];   // swizzled offset of register index j (XOR with the row's offset)
+  uint32_t soff[32];   // swizzled offset of register index j (XOR with the row's offset)
   uint32_t rowsw[16];  // swizzled offset of row bit i; a row's offset is the XOR of its set bits
 };
 
@@ -121,6 +126,8 @@ inline uint32_t tile_swizzle(uint32_t p, unsigned rho) {
 // Split sp.ops into register substages of r register bits (256 threads:
 // sp.L == r + 8).  Entry kinds let 1-qubit operations skip zero entries.
 inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
+  if (r == 0 || r > kMaxRegBits || sp.L < r || sp.L - r > 16)
+    throw std::invalid_argument("build_substages: unsupported register / row split");
   sp.r = r;
   sp.rho = rho;
   sp.subs.clear();
@@ -236,7 +243,7 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
       if (op.kind == 1) {
         so.kind = 2;
         so.dk = uint8_t(op.k);
-        for (uint32_t x = 0; x < (1u << r) && x < 16; ++x) {
+        for (uint32_t x = 0; x < (1u << r) && x < 32; ++x) {
           uint32_t idx = 0;
           for (unsigned q = 0; q < op.k; ++q)
             if (op.tbit[q] != 0xFF && ((R >> op.tbit[q]) & 1) && ((x >> reg_index(op.tbit[q])) & 1)) idx |= 1u << q;

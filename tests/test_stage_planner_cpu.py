@@ -58,7 +58,7 @@ def oracle_apply(n, gates, psi):
     return o.cheat()[1]
 
 
-@pytest.mark.parametrize("r,rho", [(0, 4), (4, 4), (3, 3), (2, 3)])
+@pytest.mark.parametrize("r,rho", [(0, 4), (5, 4), (4, 4), (3, 3), (2, 3)])
 @pytest.mark.parametrize("n,L,m,seed", [(9, 6, 3, 0), (10, 7, 4, 1), (11, 8, 5, 2), (6, 6, 3, 3), (12, 12, 5, 4)])
 def test_planned_stages_equal_gate_by_gate(lib, n, L, m, seed, r, rho):
     """r = 0 executes the per-operation stage kernel's semantics, r > 0 the
