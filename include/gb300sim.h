@@ -208,6 +208,15 @@ GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
  * fused complex64 gates of 5 to 7 targets (3xTF32 split precision). */
 GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int on);
 
+/* How set_wavefunction moves a host state that is already in the engine's
+ * precision: 1 (default) the SMs read it through the device view of
+ * page-locked host memory (gsim_host_register / cudaMallocHost, 16-byte
+ * aligned), falling back to the copy engine for pageable memory; 0 always one
+ * cudaMemcpyAsync on the copy engine.  On GB300 the SM reads held 43 ms per
+ * 8 GiB where the copy engine's first transfer after a long kernel sequence
+ * took 0.4-0.8 s. */
+GSIM_API int gsim_set_upload_mode(gsim_engine *e, int mode);
+
 /* Preallocate device memory for nqubits qubits (avoids regrowth). */
 GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
 

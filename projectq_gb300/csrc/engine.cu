@@ -666,6 +666,10 @@ class Engine {
     }
   }
   void reserve(unsigned nq) { ensure_capacity(nq); }
+  void set_upload_mode(int mode) {
+    if (mode != 0 && mode != 1) fail(GSIM_ERR_VALUE, "upload mode must be 0 (copy engine) or 1 (SM reads)");
+    upload_mode_ = mode;
+  }
   void set_tensor_cores(bool on) {
     run();
     use_tc_ = on;
@@ -923,8 +927,35 @@ class Engine {
 
   // Host <-> device transfers with precision conversion through the scratch
   // buffer, in chunks.
+  // Device view of page-locked host memory (cudaHostRegister / cudaMallocHost)
+  // covering all of [host, host + bytes), or nullptr when either end is
+  // pageable or the two ends are not one contiguous device view.
+  static const void *locked_device_view(const void *host, size_t bytes) {
+    auto view = [](const void *p) -> const char * {
+      cudaPointerAttributes a;
+      if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      return a.type == cudaMemoryTypeHost ? static_cast<const char *>(a.devicePointer) : nullptr;
+    };
+    if (!bytes) return nullptr;
+    const char *first = view(host), *last = view(static_cast<const char *>(host) + bytes - 1);
+    if (!first || !last || last - first != std::ptrdiff_t(bytes - 1)) return nullptr;
+    return first;
+  }
   void upload(const void *host, int dtype, size_t offset, size_t count) {
     const size_t hb = dtype == GSIM_C64 ? 8 : 16;
+    if (dtype == prec_ && upload_mode_ == 1) {
+      // the SMs read page-locked host memory directly (16-byte aligned buffers)
+      const void *view = locked_device_view(host, count * bpa_);
+      char *dst = static_cast<char *>(state_.p) + offset * bpa_;
+      if (view && !((reinterpret_cast<uintptr_t>(view) | reinterpret_cast<uintptr_t>(dst) | (count * bpa_)) & 15u)) {
+        CK(launch_pull(dst, view, count * bpa_, stream_));
+        CK(cudaStreamSynchronize(stream_));
+        return;
+      }
+    }
     if (dtype == prec_) {
       CK(cudaMemcpyAsync(static_cast<char *>(state_.p) + offset * bpa_, host, count * bpa_,
                          cudaMemcpyHostToDevice, stream_));
@@ -983,6 +1014,7 @@ class Engine {
   unsigned tile_bits_c64_ = kRegBitsC64 + 8, tile_bits_c128_ = kRegBitsC128 + 8;
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
+  int upload_mode_ = 1;  // host -> device state copies: 0 copy engine, 1 SM reads of page-locked memory
   bool tc_used_ = false;
   std::array<UploadSlot, 4> mslots_;
   size_t mslot_next_ = 0;
@@ -1951,6 +1983,9 @@ int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms) {
     *mode = E(e)->last_choice();
     if (pred_ms) E(e)->last_prediction(pred_ms);
   });
+}
+int gsim_set_upload_mode(gsim_engine *e, int mode) {
+  return guard([&] { E(e)->set_upload_mode(mode); });
 }
 int gsim_set_tensor_cores(gsim_engine *e, int on) {
   return guard([&] { E(e)->set_tensor_cores(on != 0); });

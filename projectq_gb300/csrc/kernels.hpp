@@ -65,6 +65,9 @@ cudaError_t launch_block_grid_sums(int prec, const void *psi, uint64_t n, unsign
                                    uint8_t *d_flags, cudaStream_t s);
 
 // Convert between storage precisions: dst_prec/src_prec 0 = c128, 1 = c64.
+// SM-driven copy (16-byte aligned pointers and size), used to read page-locked
+// host memory through its device view.
+cudaError_t launch_pull(void *dst, const void *src, uint64_t bytes, cudaStream_t s);
 cudaError_t launch_convert(int dst_prec, void *dst, int src_prec, const void *src, uint64_t n,
                            cudaStream_t s);
 

@@ -279,6 +279,13 @@ __global__ void convert_kernel(D *__restrict__ dst, const S *__restrict__ src, u
   }
 }
 
+// Copy of `bytes` bytes by the SMs: 16-byte loads from `src` (here the device
+// view of page-locked host memory) and 16-byte stores, then the 8-byte tail.
+__global__ void pull_kernel(uint4 *__restrict__ dst, const uint4 *__restrict__ src, uint64_t n16) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n16; i += stride) dst[i] = src[i];
+}
+
 // ---- Pauli expectation ---------------------------------------------------
 constexpr int kTermsPerLaunch = 8;
 struct ExpTerm {
@@ -598,6 +605,15 @@ cudaError_t launch_block_grid_sums(int prec, const void *psi, uint64_t n, unsign
     block_grid_sums_kernel<float><<<unsigned(nb), 256, 0, s>>>(static_cast<const float2 *>(psi), n, lb, d_cand, d_units, d_flags);
   else
     block_grid_sums_kernel<double><<<unsigned(nb), 256, 0, s>>>(static_cast<const double2 *>(psi), n, lb, d_cand, d_units, d_flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pull(void *dst, const void *src, uint64_t bytes, cudaStream_t s) {
+  if ((reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src) | bytes) & 15u) return cudaErrorInvalidValue;
+  const uint64_t n16 = bytes / 16;
+  if (!n16) return cudaSuccess;
+  const unsigned blocks = unsigned(std::min<uint64_t>((n16 + 511) / 512, uint64_t(sms()) * 8));
+  pull_kernel<<<blocks, 512, 0, s>>>(static_cast<uint4 *>(dst), static_cast<const uint4 *>(src), n16);
   return cudaGetLastError();
 }
 

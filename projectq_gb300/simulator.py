@@ -370,6 +370,12 @@ class Simulator:
     def synchronize(self):
         self._check(self._api.synchronize(self._h))
 
+    def set_upload_mode(self, mode="pull"):
+        """set_wavefunction transfer: "pull" (default: the SMs read page-locked
+        host memory, see pin_host; pageable arrays still use the copy engine)
+        or "copy" (always the copy engine)."""
+        self._check(self._api.set_upload_mode(self._h, {"copy": 0, "pull": 1}[mode]))
+
     def reserve(self, nqubits):
         self._check(self._api.reserve(self._h, int(nqubits)))
 

@@ -337,3 +337,29 @@ def test_gate_stream_equals_per_gate_calls(prec, fusion):
     g2.run()
     run_circuit(o2, gates[:5])
     assert_states(g2, o2, prec)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_pull_upload_of_page_locked_state(prec):
+    """set_upload_mode("pull"): the SMs read a page-locked host state through
+    its device view; the result equals the copy-engine upload, and pageable
+    or differently typed arrays fall back to the copy paths."""
+    from projectq_gb300.simulator import pin_host
+
+    n = 14
+    dt = np.complex64 if prec == "c64" else np.complex128
+    psi = random_state(n, seed=11).astype(dt)
+    g = make("gpu", seed=1, precision=prec)
+    allocate(g, n)
+    g.set_upload_mode("pull")
+    pin = pin_host(psi)
+    try:
+        g.set_wavefunction(psi, list(range(n)))
+        assert np.array_equal(g.cheat()[1].astype(dt), psi)
+    finally:
+        pin.close()
+    g.set_wavefunction(psi[::-1].copy(), list(range(n)))  # pageable: copy engine
+    assert np.array_equal(g.cheat()[1].astype(dt), psi[::-1])
+    other = random_state(n, seed=12)  # complex128 into either precision
+    g.set_wavefunction(other, list(range(n)))
+    assert np.max(np.abs(g.cheat()[1] - other)) <= TOL[prec]
