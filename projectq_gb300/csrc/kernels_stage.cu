@@ -424,16 +424,28 @@ __global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T>
 #pragma unroll
       for (int b = 0; b < 8; ++b)
         if ((row >> b) & 1) srow ^= S.rowsw[b];
+      const uint32_t o1 = S.op_end;
+      uint32_t o = S.op_begin;
+      uint32_t lx = 0;  // swaps folded into the load addresses (kind 4, first in the list)
+      for (; o < o1 && ops[o].kind == 4; ++o) {
+        const SubOpDev &op = ops[o];
+        if ((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl) lx ^= op.sdelta;
+      }
       C v[1 << R];
 #pragma unroll
-      for (int j = 0; j < (1 << R); ++j) v[j] = tile[srow ^ S.soff[j]];
-      const uint32_t o1 = S.op_end;
-      for (uint32_t o = S.op_begin; o < o1; ++o) {
+      for (int j = 0; j < (1 << R); ++j) v[j] = tile[srow ^ lx ^ S.soff[j]];
+      uint32_t sx = 0;  // swaps folded into the store addresses (kind 3)
+      for (; o < o1; ++o) {
         const SubOpDev &op = ops[o];
         if ((base & op.gctrl) != op.gctrl) continue;
         if ((row & op.tctrl) != op.tctrl) continue;
+        if (op.kind == 3) {
+          sx ^= op.sdelta;
+          continue;
+        }
         reg_apply<T, R>(v, op, pool + op.mat, row, base);
       }
+      srow ^= sx;
 #pragma unroll
       for (int j = 0; j < (1 << R); ++j) tile[srow ^ S.soff[j]] = v[j];
       __syncthreads();

@@ -71,7 +71,7 @@ constexpr unsigned kRegBitsC64 = 5, kRegBitsC128 = 3, kMaxRegBits = 5;
 struct alignas(16) SubOpDev {
   uint8_t jidx[32]; // diagonal: index bits contributed by the register qubits, per j (16-byte aligned)
   uint64_t gctrl;   // non-local controls (global mask)
-  uint32_t kind;    // 0 dense 1-qubit, 1 dense 2-qubit, 2 diagonal
+  uint32_t kind;    // 0 dense 1-qubit, 1 dense 2-qubit, 2 diagonal, 3 / 4 swap folded into the stores / loads
   uint32_t mat;     // offset in the stage's pool
   uint32_t jctrl;   // controls among the register bits (mask over j)
   uint32_t tctrl;   // controls among the row bits (mask over the row index)
@@ -86,7 +86,9 @@ struct alignas(16) SubOpDev {
   uint8_t dreg;     // diagonal: number of its qubits that are register bits
   uint32_t amask;   // dense: register indices j that are group bases with the controls satisfied
   uint8_t dq, dB;   // diagonal with dreg == 1: that qubit's index bit and register bit
-  uint8_t pad[10];
+  uint8_t pad[2];
+  uint32_t sdelta;  // kinds 3, 4 (a swap folded into the stores / loads): the address XOR, soff[1 << B]
+  uint32_t pad2;
 };
 static_assert(sizeof(SubOpDev) % 16 == 0, "SubOpDev must keep 16-byte alignment in arrays");
 static_assert(offsetof(SubOpDev, jidx) == 0, "jidx is read with 16-byte loads");
@@ -286,6 +288,58 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
           if (!(x & tm) && (x & so.jctrl) == so.jctrl) so.amask |= 1u << x;
       }
       sp.sops.push_back(so);
+    }
+    // An X on register bit B whose controls are all row or non-local bits is
+    // not applied to the registers when no other operation of the substage
+    // touches B before it (then it is folded into the loads, kind 4) or after
+    // it (folded into the stores, kind 3): it only exchanges where j and
+    // j ^ (1 << B) live, and since soff is linear that is an XOR of
+    // soff[1 << B] on every load or store address of the threads whose
+    // controls hold.  Folded loads go first in the list, folded stores last.
+    {
+      auto regs_of = [](const SubOpDev &so) {
+        uint32_t regs = so.jctrl;
+        if (so.kind == 2) {
+          for (unsigned q = 0; q < so.dk; ++q)
+            if (so.dloc[q] == 0) regs |= 1u << so.didx[q];
+        } else {
+          regs |= 1u << so.rb[0];
+          if (so.kind == 1) regs |= 1u << so.rb[1];
+        }
+        return regs;
+      };
+      auto foldable = [](const SubOpDev &so) { return so.kind == 0 && so.swap && so.jctrl == 0; };
+      const size_t b0 = sd.op_begin;
+      std::vector<SubOpDev> front, mid, back;
+      uint32_t earlier = 0;
+      for (size_t i = b0; i < sp.sops.size(); ++i) {
+        SubOpDev so = sp.sops[i];
+        if (foldable(so) && !((earlier >> so.rb[0]) & 1)) {
+          so.kind = 4;
+          so.sdelta = sd.soff[1u << so.rb[0]];
+          front.push_back(so);
+        } else {
+          earlier |= regs_of(so);
+          mid.push_back(so);
+        }
+      }
+      std::vector<SubOpDev> kept;
+      uint32_t later = 0;
+      for (size_t i = mid.size(); i-- > 0;) {
+        SubOpDev so = mid[i];
+        if (foldable(so) && !((later >> so.rb[0]) & 1)) {
+          so.kind = 3;
+          so.sdelta = sd.soff[1u << so.rb[0]];
+          back.push_back(so);
+        } else {
+          later |= regs_of(so);
+          kept.push_back(so);
+        }
+      }
+      sp.sops.resize(b0);
+      sp.sops.insert(sp.sops.end(), front.begin(), front.end());
+      sp.sops.insert(sp.sops.end(), kept.rbegin(), kept.rend());
+      sp.sops.insert(sp.sops.end(), back.begin(), back.end());
     }
     sd.op_end = uint32_t(sp.sops.size());
     sp.subs.push_back(sd);

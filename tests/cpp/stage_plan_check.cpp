@@ -108,11 +108,24 @@ void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::Stag
         for (unsigned b = 0; b < L - r; ++b)
           if ((row >> b) & 1) srow ^= S.rowsw[b];
         std::vector<cplx> v(size_t(1) << r);
-        for (uint32_t j = 0; j < v.size(); ++j) v[j] = smem[srow ^ S.soff[j]];
-        for (uint32_t o = S.op_begin; o < S.op_end; ++o) {
+        uint32_t o = S.op_begin, lx = 0;
+        for (; o < S.op_end && sp.sops[o].kind == 4; ++o) {  // swaps folded into the load addresses
           const gsim::SubOpDev &op = sp.sops[o];
+          if (op.sdelta != S.soff[1u << op.rb[0]]) g_inconsistent = true;
+          if ((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl) lx ^= op.sdelta;
+        }
+        for (uint32_t j = 0; j < v.size(); ++j) v[j] = smem[srow ^ lx ^ S.soff[j]];
+        uint32_t sx = 0;
+        for (; o < S.op_end; ++o) {
+          const gsim::SubOpDev &op = sp.sops[o];
+          if (op.kind == 4) g_inconsistent = true;  // load folds must lead the list
           if ((base & op.gctrl) != op.gctrl) continue;
           if ((row & op.tctrl) != op.tctrl) continue;
+          if (op.kind == 3) {  // swap folded into the store addresses
+            if (op.sdelta != S.soff[1u << op.rb[0]]) g_inconsistent = true;
+            sx ^= op.sdelta;
+            continue;
+          }
           const cplx *M = sp.pool.data() + op.mat;
           if (op.kind == 2) {
             // the kernel's three paths: one factor (no register qubit), two
@@ -183,7 +196,7 @@ void apply_stage_substages(std::vector<cplx> &psi, unsigned nq, const gsim::Stag
             }
           }
         }
-        for (uint32_t j = 0; j < v.size(); ++j) smem[srow ^ S.soff[j]] = v[j];
+        for (uint32_t j = 0; j < v.size(); ++j) smem[srow ^ sx ^ S.soff[j]] = v[j];
       }
     }
     for (size_t p = 0; p < TS; ++p) psi[gidx(p)] = smem[gsim::tile_swizzle(uint32_t(p), sp.rho)];
