@@ -495,7 +495,9 @@ def run_learned(a):
     in 20..30 complex64, depth 10..200, the config-5 gate mix, 10% ending
     with the time evolution of a 50-term Pauli Hamiltonian): host wall time
     with the shipped cost model against the greedy fixed-size fusion and the
-    stage planner, and 1 - F of the learned result against the greedy one."""
+    stage planner, and 1 - F of the learned result against the greedy one;
+    then the same comparison on block-local circuits (26-30 qubits), where the
+    model's own tensor-core clusters compete with the stage plan."""
     from projectq_gb300 import costmodel
 
     shipped = costmodel.load()
@@ -504,9 +506,15 @@ def run_learned(a):
     for r in res["rows"]:
         choices[r["choice"]] = choices.get(r["choice"], 0) + 1
     rows = res.pop("rows")
+    blk = costmodel.evaluate_blocked(shipped["params"], shipped["regimes_c64"])
+    blk_rows = blk.pop("rows")
+
+    def rnd(r):
+        return {k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
+
     print(json.dumps({"workload": "learned fusion planner vs greedy fixed-size fusion", **res, "choices": choices,
-                      "per_circuit": [{k: (round(v, 5) if isinstance(v, float) else v) for k, v in r.items()}
-                                      for r in rows]}), flush=True)
+                      "per_circuit": [rnd(r) for r in rows],
+                      "local_block_circuits": {**rnd(blk), "per_circuit": [rnd(r) for r in blk_rows]}}), flush=True)
 
 
 def main():

@@ -137,6 +137,23 @@ def random_circuit(rng, n, depth):
     return gates
 
 
+def blocked_circuit(rng, n, block, per_block):
+    """A circuit with locality: for each block of `block` neighbouring qubits
+    in turn, `per_block` gates inside the block (60% Rx/Ry/Rz, 40% CNOT).
+    Whole blocks fit one tensor-core cluster of up to 7 qubits, so here the
+    learned planner's own clusters compete with the stage plan."""
+    gates = []
+    for b0 in range(0, n - block + 1, block):
+        for _ in range(per_block):
+            if rng.uniform() < 0.6:
+                q = int(rng.integers(b0, b0 + block))
+                gates.append(((Rx, Ry, Rz)[int(rng.integers(3))](float(rng.uniform(0, 2 * np.pi))), (q,), ()))
+            else:
+                a, c = (int(v) for v in rng.choice(np.arange(b0, b0 + block), 2, replace=False))
+                gates.append((X, (a,), (c,)))
+    return gates
+
+
 def launch_features(records, api=None):
     """Features (n x 16) of launch records (dicts of profile_records or
     LaunchRecord structs), computed by the engine's own gsim_launch_features."""
@@ -323,6 +340,30 @@ def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=30, dmin=10, dmax=200
         res["max_one_minus_fidelity"] = max(r["one_minus_fidelity"] for r in rows)
     res["rows"] = rows
     return res
+
+
+def evaluate_blocked(params, regimes, sizes=(26, 28, 30), blocks=((7, 40), (6, 30), (5, 20)), seed=3,
+                     precision="c64"):
+    """Wall time of the learned planner against the stage plan and the greedy
+    fixed-size fusion on block-local circuits (best of two runs each)."""
+    rows = []
+    for n in sizes:
+        for block, per in blocks:
+            gates = blocked_circuit(np.random.default_rng(seed * 1000 + n * 10 + block), n, block, per)
+            row = {"n": n, "block": block, "gates": len(gates)}
+            for mode in ("reference", "staged", "learned"):
+                best, choice = math.inf, None
+                for _ in range(2):
+                    t, ch = wall_time(n, gates, mode, precision, params, regimes)
+                    best = min(best, t)
+                    choice = ch if ch is not None else choice
+                row[("greedy" if mode == "reference" else mode) + "_s"] = best
+                if mode == "learned":
+                    row["choice"] = CHOICES.get(choice, str(choice))
+            rows.append(row)
+    tot = {k: sum(r[k] for r in rows) for k in ("greedy_s", "staged_s", "learned_s")}
+    return {"circuits": len(rows), **tot, "speedup_vs_greedy": tot["greedy_s"] / tot["learned_s"],
+            "speedup_vs_staged": tot["staged_s"] / tot["learned_s"], "rows": rows}
 
 
 def main():
