@@ -161,3 +161,27 @@ def test_shipped_cost_model_beats_greedy_fusion():
         msg = {k: v for k, v in res.items() if k != "rows"}
         assert res["learned_s"] < res["greedy_s"] / 1.2, msg
         assert res["max_one_minus_fidelity"] <= (1e-9 if prec == "c64" else 1e-12), msg
+
+
+@pytest.mark.skipif(not cm.DATA.exists(), reason="no trained cost model shipped")
+def test_learned_planner_uses_its_clusters_on_block_local_circuits():
+    """Where the network's choice differs from the stage plan: on a 30-qubit
+    circuit of 40-gate blocks over 7 neighbouring qubits it predicts its own
+    tensor-core clusters (one launch per block) to be faster, runs them, and
+    is not slower than the stage plan in measured wall time (5% noise
+    allowed); the states agree."""
+    shipped = cm.load()
+    n = 30
+    gates = cm.blocked_circuit(np.random.default_rng(3 * 1000 + n * 10 + 7), n, 7, 40)
+    t_staged, _, s_staged = cm.wall_time(n, gates, "staged", "c64", keep=True)
+    t_learned, choice, s_learned = cm.wall_time(n, gates, "learned", "c64", shipped["params"],
+                                                 shipped["regimes_c64"], keep=True)
+    ip, _ = s_staged.compare(s_learned)
+    n1, n2 = s_staged.compare(s_staged)[0].real, s_learned.compare(s_learned)[0].real
+    s_staged.close()
+    s_learned.close()
+    assert cm.CHOICES[choice] == "model clusters"
+    assert 1 - abs(ip) ** 2 / (n1 * n2) < 1e-9
+    t_staged = min(t_staged, cm.wall_time(n, gates, "staged", "c64")[0])
+    t_learned = min(t_learned, cm.wall_time(n, gates, "learned", "c64", shipped["params"], shipped["regimes_c64"])[0])
+    assert t_learned <= 1.05 * t_staged, (t_learned, t_staged)
