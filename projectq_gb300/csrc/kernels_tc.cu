@@ -15,9 +15,10 @@
 //
 // The kernel is persistent (one CTA per SM) and warp-specialised:
 //   warps 0-7   producers: gather 16 amplitudes of a group per K-chunk from
-//               HBM (two threads per group, loads of the next chunk issued
-//               before the current one is converted), split them into TF32
-//               hi/lo and write both into a ring of shared-memory stages;
+//               HBM (two threads per group, the loads of the next kPrefetch
+//               chunks in flight; 16-byte pair loads when a target is bit 0),
+//               split them into TF32 hi/lo and write both into a ring of
+//               shared-memory stages;
 //   warps 8-11  epilogue: read a finished accumulator from TMEM
 //               (tcgen05.ld, warp w owns TMEM lanes 32*(w%4)..) and store the
 //               outputs back in place;
@@ -53,7 +54,8 @@ constexpr int kProducers = 256;    // warps 0-7
 constexpr int kEpilogue = 128;     // warps 8-11
 constexpr int kMmaWarp = 12;
 constexpr int kLoaderWarp = 13;
-constexpr int kPrefetch = 4;       // K-chunks of loads in flight per producer thread
+constexpr int kPrefetch = 4;       // K-chunks of loads in flight per producer thread (6 measured slower:
+                                   // spills at k = 5 and no gain at k = 6, 7)
 constexpr uint32_t kStageA = uint32_t(kRows) * kKC * 4u;  // one split (hi or lo) of an A chunk
 
 template <int KQ>
