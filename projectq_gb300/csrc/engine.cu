@@ -1154,8 +1154,14 @@ std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) c
   std::vector<PlanStep> steps = planner.plan(gates);
   // Register substages where the tile is 2^(r + 8) amplitudes (256 threads).
   const unsigned r = prec_ == GSIM_C64 ? kRegBitsC64 : kRegBitsC128, rho = prec_ == GSIM_C64 ? 4 : 3;
-  for (auto &st : steps)
-    if (st.is_stage && use_reg_stages_ && st.stage.L == r + 8) build_substages(st.stage, r, rho);
+  for (auto &st : steps) {
+    if (!(st.is_stage && use_reg_stages_ && st.stage.L == r + 8)) continue;
+    build_substages(st.stage, r, rho);
+    if (stage_subs_bytes(st.stage) + st.stage.sops.size() * sizeof(SubOpDev) > kStageTableBytes) {
+      st.stage.subs.clear();  // descriptors too large for the kernel parameter
+      st.stage.sops.clear();
+    }
+  }
   return steps;
 }
 

@@ -22,6 +22,10 @@
 namespace gsim {
 namespace {
 
+struct alignas(16) StageTable {
+  unsigned char bytes[kStageTableBytes];  // [SubstageDev...][SubOpDev...] of one stage
+};
+
 struct StageArgs {
   uint64_t ntiles;
   uint32_t L, m, h, nops;
@@ -359,12 +363,14 @@ __device__ __forceinline__ void reg_apply(cplx_t<T> (&v)[1 << R], const SubOpDev
 
 template <typename T, int R>
 __global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T> *__restrict__ psi, const __grid_constant__ StageArgs A,
-                                                        const unsigned char *__restrict__ table, uint32_t nsubs,
-                                                        uint32_t sops_off, uint32_t pool_off, uint32_t table_bytes,
-                                                        uint32_t rho) {
-  // Shared memory: the tile (2^L amplitudes, swizzled), the segment offsets,
-  // then a copy of the stage's table (substages, operations, matrices) so the
-  // per-operation reads are shared-memory broadcasts.
+                                                        const __grid_constant__ StageTable Tb,
+                                                        const unsigned char *__restrict__ pool_src, uint32_t nsubs,
+                                                        uint32_t sops_off, uint32_t pool_bytes, uint32_t rho) {
+  // The substage and operation descriptors are read from the kernel parameter
+  // (constant bank): every thread of a warp reads the same descriptor, so the
+  // per-operation control flow runs on warp-uniform values.  Shared memory:
+  // the tile (2^L amplitudes, swizzled), the segment offsets, then a copy of
+  // the matrices and diagonal tables (indexed per thread).
   using C = cplx_t<T>;
   constexpr uint32_t TS = 1u << (R + 8);
   constexpr int PER = sizeof(T) == 4 ? TS / 512 : TS / 256;  // 16-byte loads per thread per tile
@@ -380,12 +386,12 @@ __global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T>
       if ((s >> b) & 1) o |= uint64_t(1) << A.lpos[A.m + b];
     segoff[s] = o;
   }
-  for (uint32_t i = threadIdx.x; i < table_bytes / 16; i += blockDim.x)
-    reinterpret_cast<uint4 *>(tab)[i] = reinterpret_cast<const uint4 *>(table)[i];
+  for (uint32_t i = threadIdx.x; i < pool_bytes / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(tab)[i] = reinterpret_cast<const uint4 *>(pool_src)[i];
   __syncthreads();
-  const SubstageDev *subs = reinterpret_cast<const SubstageDev *>(tab);
-  const SubOpDev *ops = reinterpret_cast<const SubOpDev *>(tab + sops_off);
-  const C *pool = reinterpret_cast<const C *>(tab + pool_off);
+  const SubstageDev *subs = reinterpret_cast<const SubstageDev *>(Tb.bytes);
+  const SubOpDev *ops = reinterpret_cast<const SubOpDev *>(Tb.bytes + sops_off);
+  const C *pool = reinterpret_cast<const C *>(tab);
   const uint32_t row = threadIdx.x;
   const uint32_t mask = (1u << A.m) - 1;
   constexpr uint32_t RHO = sizeof(T) == 4 ? 4u : 3u;  // the planner's bank-class bits (checked at launch)
@@ -506,9 +512,13 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
       return cudaErrorInvalidValue;
     const uint32_t sops_off = uint32_t(stage_subs_bytes(plan));
     const uint32_t pool_off = sops_off + uint32_t((plan.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16);
-    const uint32_t table_bytes = pool_off + uint32_t((plan.pool.size() * sizeof(cplx_t<T>) + 15) / 16 * 16);
+    const uint32_t pool_bytes = uint32_t((plan.pool.size() * sizeof(cplx_t<T>) + 15) / 16 * 16);
+    if (sops_off + plan.sops.size() * sizeof(SubOpDev) > kStageTableBytes) return cudaErrorInvalidValue;
+    thread_local StageTable tb;  // host staging of the kernel parameter (copied at launch)
+    std::memcpy(tb.bytes, plan.subs.data(), plan.subs.size() * sizeof(SubstageDev));
+    std::memcpy(tb.bytes + sops_off, plan.sops.data(), plan.sops.size() * sizeof(SubOpDev));
     const size_t smem_reg = (size_t(1) << A.L) * sizeof(cplx_t<T>) + (((size_t(1) << A.h) * 8 + 15) & ~size_t(15)) +
-                            table_bytes;
+                            pool_bytes;
     if (smem_reg > 200 * 1024) return cudaErrorInvalidValue;
     static bool reg_attr = false;
     if (!reg_attr) {
@@ -519,10 +529,9 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_reg_kernel<T, R>, 256, smem_reg);
     per_sm = std::max(1, per_sm);
     const uint64_t grid = std::min<uint64_t>(A.ntiles, uint64_t(stage_sms()) * per_sm);
-    stage_reg_kernel<T, R><<<unsigned(grid), 256, smem_reg, s>>>(static_cast<cplx_t<T> *>(psi), A,
-                                                                 static_cast<const unsigned char *>(d_ops),
-                                                                 uint32_t(plan.subs.size()), sops_off, pool_off,
-                                                                 table_bytes, plan.rho);
+    stage_reg_kernel<T, R><<<unsigned(grid), 256, smem_reg, s>>>(
+        static_cast<cplx_t<T> *>(psi), A, tb, static_cast<const unsigned char *>(d_ops) + pool_off,
+        uint32_t(plan.subs.size()), sops_off, pool_bytes, plan.rho);
     return cudaGetLastError();
   }
   int per_sm = 1;

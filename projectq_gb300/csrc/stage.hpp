@@ -67,6 +67,10 @@ struct StageOpDev {
 // Register bits per thread of the register-substage kernel (tile = 2^(r + 8)
 // amplitudes, 256 threads): 32 complex64 / 8 complex128 amplitudes per thread.
 constexpr unsigned kRegBitsC64 = 5, kRegBitsC128 = 3, kMaxRegBits = 5;
+// Substage and operation descriptors of one register stage travel as a kernel
+// parameter (constant bank: warp-uniform reads); stages whose descriptors
+// exceed this run on the one-pass-per-operation kernel instead.
+constexpr size_t kStageTableBytes = 24576;
 
 struct alignas(16) SubOpDev {
   uint8_t jidx[32]; // diagonal: index bits contributed by the register qubits, per j (16-byte aligned)
