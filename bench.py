@@ -243,7 +243,7 @@ def host_memory_gib():
 
 
 def run_reference(a):
-    """--impl reference: the CPU implementation on the machine's host cores."""
+    """--impl reference: the CPU implementation on this machine's host cores."""
     from projectq_gb300.workloads import config2_circuit
 
     rank = int(os.environ.get("RANK", "0"))

@@ -8,7 +8,7 @@
 // the tests can drive the CUDA engine and this oracle with the same calls.
 //
 // Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
-// this library, and only as the checker or the CPU baseline.  The product
+// this library, and only to check results or as the CPU baseline.  The product
 // path (libgb300sim.so) never links or calls it.
 //
 // Parity pins: tests/test_oracle_cpu.py checks this oracle against the

@@ -14,7 +14,7 @@ plans of each flush -- the greedy fixed-size clusters of the reference's rule,
 clusters whose boundaries the model chooses (a gate joins the open cluster
 when the merged launch is predicted cheaper than two launches), and the
 stage plan -- and runs the cheapest.  The greedy fixed-size fusion is the
-fallback and the judge: `calibrate` measures wall time of learned against
+fallback and the yardstick: `calibrate` measures wall time of learned against
 greedy per state size on circuits not used for training, and the engine
 runs learned plans only on the state sizes where they won
 (gsim_set_learned_regimes); everywhere else, and with no model installed,
@@ -285,7 +285,7 @@ def _stream(rng, n, dmin, dmax, p_tail=0.1):
 
 
 def calibrate(params, per_size=3, sizes=range(18, 31), precisions=("c64", "c128"), seed=7, dmin=10, dmax=120):
-    """The judge: per state size, total wall time of learned against greedy
+    """The yardstick: per state size, total wall time of learned against greedy
     fixed-size fusion on `per_size` random circuits (not the training ones);
     returns {precision: uint8[65]} with 1 where learned was faster."""
     out = {}
@@ -371,7 +371,7 @@ def main():
     ap.add_argument("--collect", type=int, default=60)
     ap.add_argument("--train", action="store_true")
     ap.add_argument("--epochs", type=int, default=4000)
-    ap.add_argument("--calibrate", type=int, default=0, help="circuits per state size for the judge")
+    ap.add_argument("--calibrate", type=int, default=0, help="circuits per state size for the calibration against greedy fusion")
     ap.add_argument("--evaluate", type=int, default=0)
     ap.add_argument("--out", default=str(DATA))
     a = ap.parse_args()
