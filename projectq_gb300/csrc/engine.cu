@@ -562,17 +562,37 @@ class Engine {
     CK(cudaMemcpyAsync(psi, state_.p, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
     std::vector<DevBuf> ck;
     std::vector<int> ck_at(gates.size(), -1);  // checkpoint index holding the state after gate i
-    for (size_t i = 0; i < gates.size(); ++i) {
-      DenseOp op;
-      op.m.assign(gates[i].u, gates[i].u + 4);
-      op.pos = {gates[i].target};
-      op.ctrl_mask = gates[i].ctrl_mask;
-      CK(launch_dense(prec_, psi, N_, op, stream_));
-      if (ckpt && (i + 1) % ckpt == 0 && i + 1 < gates.size()) {
-        ck.emplace_back();
-        void *c = ck.back().get(n * bpa_);
-        CK(cudaMemcpyAsync(c, psi, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
-        ck_at[i] = int(ck.size()) - 1;
+    // Forward pass with the stage planner, one plan per segment between
+    // checkpoints (the planner's passes end exactly at a segment's last
+    // gate).  The stage executor works on state_, so the forward copy takes
+    // its place for the duration.
+    struct SwapBack {  // restores state_ also when a launch fails
+      DevBuf &a, &b;
+      SwapBack(DevBuf &x, DevBuf &y) : a(x), b(y) { std::swap(a, b); }
+      ~SwapBack() { std::swap(a, b); }
+    };
+    {
+      SwapBack forward_on_copy(state_, aux1_);
+      for (size_t s0 = 0; s0 < gates.size();) {
+        const size_t s1 = ckpt ? std::min(gates.size(), s0 + ckpt) : gates.size();
+        std::vector<StageGate> seg;
+        seg.reserve(s1 - s0);
+        for (size_t i = s0; i < s1; ++i) {
+          StageGate g;
+          g.m.assign(gates[i].u, gates[i].u + 4);
+          g.pos = {gates[i].target};
+          g.ctrl_mask = gates[i].ctrl_mask;
+          seg.push_back(std::move(g));
+        }
+        std::vector<PlanStep> steps = plan_staged(seg);
+        execute_staged(steps);
+        if (ckpt && s1 < gates.size()) {
+          ck.emplace_back();
+          void *c = ck.back().get(n * bpa_);
+          CK(cudaMemcpyAsync(c, state_.p, n * bpa_, cudaMemcpyDeviceToDevice, stream_));
+          ck_at[s1 - 1] = int(ck.size()) - 1;
+        }
+        s0 = s1;
       }
     }
     std::vector<PauliApplyTermDev> dev(terms.size());
