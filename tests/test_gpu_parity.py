@@ -363,3 +363,46 @@ def test_pull_upload_of_page_locked_state(prec):
     other = random_state(n, seed=12)  # complex128 into either precision
     g.set_wavefunction(other, list(range(n)))
     assert np.max(np.abs(g.cheat()[1] - other)) <= TOL[prec]
+
+
+def test_headline_circuit_precision_form():
+    """The 30-qubit headline circuit's family at 22 qubits: complex64 with FP64
+    reductions (stage planner) against the complex128 path and the CPU oracle:
+    1 - F <= 1e-6 (the stated bar; measured ~1e-12) and expectation values
+    within 1e-6."""
+    from projectq_gb300.workloads import config2_circuit
+
+    n = 22
+    gates = config2_circuit(n, depth=40, per_layer=40, seed=0)
+    psi0 = random_state(n, seed=0)
+    states, ev = {}, {}
+    zz = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
+    for key, kind, prec, fusion in (("c64", "gpu", "c64", "staged"), ("c128", "gpu", "c128", "staged"),
+                                    ("oracle", "oracle", "c128", "reference")):
+        s = make(kind, seed=1, precision=prec, fusion=fusion)
+        allocate(s, n)
+        s.set_wavefunction(psi0, list(range(n)))
+        run_circuit(s, gates)
+        ev[key] = s.get_expectation_value(zz, list(range(n)))
+        states[key] = s.cheat()[1]
+    ref = states["oracle"]
+    assert np.max(np.abs(states["c128"] - ref)) < 1e-12
+    for key in ("c64", "c128"):
+        f = abs(np.vdot(ref, states[key])) ** 2 / (np.vdot(ref, ref).real * np.vdot(states[key], states[key]).real)
+        assert 1 - f <= 1e-6, (key, 1 - f)
+        assert abs(ev[key] - ev["oracle"]) <= 1e-6
+
+
+@pytest.mark.parametrize("kmax", [1, 2, 3, 6, 7])
+def test_greedy_fusion_width(kmax):
+    """set_fusion("reference", kmax): the greedy fixed-size rule with clusters
+    of up to kmax qubits (complex64 clusters of 5-7 run on tensor cores)
+    applies the same gates as the oracle."""
+    n = 16
+    gates = random_mixed_circuit(n, 120, 21 + kmax, kmax=3, max_ctrl=2)
+    for prec in PRECS:
+        g, o = pair(n, prec)
+        g.set_fusion("reference", kmax)
+        run_circuit(g, gates)
+        run_circuit(o, gates)
+        assert_states(g, o, prec, tol=TOL[prec] * (4 if prec == "c64" else 1))
