@@ -407,6 +407,11 @@ def run_gates(a):
         "2q_dense": lambda q, n: (np.kron(Rx(0.2), H), [q, (q + 11) % n], []),
         "3q_dense": lambda q, n: (np.kron(np.kron(Rx(0.2), H), Rx(0.5)), [q, (q + 11) % n, (q + 19) % n], []),
     }
+    wide = {  # CUDA-core wide-gate kernel (tensor cores off): compute-bound, reported with its FLOP rate
+        "7q_dense_cuda_cores": lambda q, n: (haar7, [(q + 4 * i) % n for i in range(7)], []),
+    }
+    haar7 = np.linalg.qr(np.random.default_rng(7).standard_normal((128, 128))
+                         + 1j * np.random.default_rng(8).standard_normal((128, 128)))[0]
     for prec in ("c64", "c128"):
         sim = Simulator(1, precision=prec, fusion="none")
         for q in range(nq):
@@ -418,6 +423,14 @@ def run_gates(a):
             mean = float(np.mean(gbs)) if gbs else 0.0
             out[f"{prec}/{name}"] = {"launches": len(recs), "gbs_mean": round(mean, 1), "gbs_min": round(min(gbs), 1),
                                      "frac_of_peak": round(mean / peak, 3)}
+        sim.set_tensor_cores(False)
+        for name, mk in wide.items():
+            gates = [mk(q, nq) for q in range(0, nq, 5)]
+            ms, cnt, recs = timed_steps(sim, gates, 1, 1, None)
+            per = [r["ms"] for r in recs if r["ms"] > 0]
+            tflops = 8.0 * 2 ** nq * 128 / (np.mean(per) * 1e-3) / 1e12 if per else 0.0
+            out[f"{prec}/{name}"] = {"launches": len(recs), "ms_mean": round(float(np.mean(per)), 3),
+                                     "algorithmic_tflops": round(tflops, 2)}
         sim.close()
     print(json.dumps({"workload": "single-gate kernels, one pass per gate", "qubits": nq, "peak_gbs": peak,
                       "kernels": out}), flush=True)

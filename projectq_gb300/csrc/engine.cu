@@ -819,7 +819,10 @@ class Engine {
       tc_used_ = true;
     } else if (route == 2) {
       const size_t D = size_t(1) << op.pos.size();
-      void *dm = upload_matrix(op.m, D * D);
+      std::vector<cplx> mt(D * D);  // the wide kernel reads U transposed
+      for (size_t r = 0; r < D; ++r)
+        for (size_t j = 0; j < D; ++j) mt[j * D + r] = op.m[r * D + j];
+      void *dm = upload_matrix(mt, D * D);
       CK(launch_wide(prec_, state_.p, N_, op, dm, stream_));
     } else {
       CK(launch_dense(prec_, state_.p, N_, op, stream_));

@@ -24,8 +24,9 @@ size_t tc_operand_floats(int k);
 DenseOp tc_sorted_targets(const DenseOp &op);
 void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out);
 cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s);
-// Gates of up to 7 targets; d_matrix: the 2^k x 2^k matrix (row-major) in the
-// state's precision in device memory.
+// Gates of 5 to 7 targets on CUDA cores; d_matrix: the 2^k x 2^k matrix
+// TRANSPOSED (column j contiguous: element [j][r] = U[r][j]) in the state's
+// precision in device memory.
 cudaError_t launch_wide(int prec, void *psi, unsigned nq, const DenseOp &op, const void *d_matrix,
                         cudaStream_t s);
 

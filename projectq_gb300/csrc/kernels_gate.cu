@@ -113,38 +113,50 @@ __global__ void __launch_bounds__(256) dense_kernel_vec2(float2 *__restrict__ ps
 struct WideArgs {
   uint64_t units;      // number of groups
   uint64_t ctrl_set;
-  int nins, k, gpb;    // insert count, targets, groups per block
+  int nins, k;         // insert count, targets
   uint8_t ins[64];
   uint64_t off[128];   // offset of matrix index j
 };
 
+// Gates of k >= 5 targets on CUDA cores.  A block has D = 2^k threads, one per
+// output row r, and takes kWideGroups amplitude groups at a time: the groups
+// are gathered into shared memory, then every thread walks the columns j
+// reading U^T[j][r] (consecutive r: coalesced, and reused for all the
+// groups) and the group inputs x[g][j] (shared-memory broadcasts).
+constexpr int kWideGroups = 8;
+
 template <typename T>
-__global__ void __launch_bounds__(256) wide_kernel(cplx_t<T> *__restrict__ psi, const cplx_t<T> *__restrict__ U,
+__global__ void __launch_bounds__(128) wide_kernel(cplx_t<T> *__restrict__ psi, const cplx_t<T> *__restrict__ Ut,
                                                    const __grid_constant__ WideArgs A) {
   extern __shared__ __align__(16) unsigned char smem_w[];
   cplx_t<T> *buf = reinterpret_cast<cplx_t<T> *>(smem_w);
   const int D = 1 << A.k;
-  const int gl = threadIdx.x / D, r = threadIdx.x % D;  // local group, output row
-  for (uint64_t g0 = uint64_t(blockIdx.x) * A.gpb; g0 < A.units; g0 += uint64_t(gridDim.x) * A.gpb) {
-    const uint64_t g = g0 + gl;
-    const bool active = gl < A.gpb && g < A.units;
-    uint64_t base = 0;
-    if (active) {
-      base = insert_zeros(g, A.ins, A.nins) | A.ctrl_set;
-      buf[gl * D + r] = psi[base + A.off[r]];
+  const int r = threadIdx.x;  // blockDim.x == D
+  for (uint64_t g0 = uint64_t(blockIdx.x) * kWideGroups; g0 < A.units;
+       g0 += uint64_t(gridDim.x) * kWideGroups) {
+    uint64_t base[kWideGroups];
+#pragma unroll
+    for (int g = 0; g < kWideGroups; ++g) {
+      const uint64_t gg = g0 + uint64_t(g);
+      base[g] = gg < A.units ? (insert_zeros(gg, A.ins, A.nins) | A.ctrl_set) : 0;
+      buf[g * D + r] = gg < A.units ? psi[base[g] + A.off[r]] : mkc<T>(T(0), T(0));
     }
     __syncthreads();
-    if (active) {
-      T re = T(0), im = T(0);
-      const cplx_t<T> *row = U + size_t(r) * D;
-      const cplx_t<T> *v = buf + gl * D;
-      for (int j = 0; j < D; ++j) {
-        const cplx_t<T> m = __ldg(row + j), x = v[j];
-        re = fma(m.x, x.x, fma(-m.y, x.y, re));
-        im = fma(m.x, x.y, fma(m.y, x.x, im));
+    T re[kWideGroups], im[kWideGroups];
+#pragma unroll
+    for (int g = 0; g < kWideGroups; ++g) re[g] = im[g] = T(0);
+    for (int j = 0; j < D; ++j) {
+      const cplx_t<T> m = __ldg(Ut + size_t(j) * D + r);
+#pragma unroll
+      for (int g = 0; g < kWideGroups; ++g) {
+        const cplx_t<T> x = buf[g * D + j];
+        re[g] = fma(m.x, x.x, fma(-m.y, x.y, re[g]));
+        im[g] = fma(m.x, x.y, fma(m.y, x.x, im[g]));
       }
-      psi[base + A.off[r]] = mkc<T>(re, im);
     }
+#pragma unroll
+    for (int g = 0; g < kWideGroups; ++g)
+      if (g0 + uint64_t(g) < A.units) psi[base[g] + A.off[r]] = mkc<T>(re[g], im[g]);
     __syncthreads();
   }
 }
@@ -245,10 +257,11 @@ cudaError_t launch_wide_t(void *psi, unsigned nq, const DenseOp &op, const void 
     for (int l = 0; l < k; ++l)
       if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
   A.units = uint64_t(1) << (nq - ins.size());
-  A.gpb = std::max(1, 256 / D);
-  const size_t smem = size_t(A.gpb) * D * sizeof(cplx_t<T>);
-  const uint64_t blocks = std::min<uint64_t>((A.units + A.gpb - 1) / A.gpb, uint64_t(num_sms()) * 8);
-  wide_kernel<T><<<unsigned(std::max<uint64_t>(1, blocks)), 256, smem, s>>>(
+  if (k < 5 || k > 7) throw std::invalid_argument("the wide-gate kernel takes 5 to 7 targets");
+  const size_t smem = size_t(kWideGroups) * D * sizeof(cplx_t<T>);
+  const uint64_t blocks =
+      std::min<uint64_t>((A.units + kWideGroups - 1) / kWideGroups, uint64_t(num_sms()) * (2048 / D));
+  wide_kernel<T><<<unsigned(std::max<uint64_t>(1, blocks)), unsigned(D), smem, s>>>(
       static_cast<cplx_t<T> *>(psi), static_cast<const cplx_t<T> *>(d_matrix), A);
   return cudaGetLastError();
 }
