@@ -406,8 +406,12 @@ def run_gates(a):
         "cnot": lambda q, n: (X, [q], [(q + 7) % n]),
         "2q_dense": lambda q, n: (np.kron(Rx(0.2), H), [q, (q + 11) % n], []),
         "3q_dense": lambda q, n: (np.kron(np.kron(Rx(0.2), H), Rx(0.5)), [q, (q + 11) % n, (q + 19) % n], []),
+        "4q_dense": lambda q, n: (haar4, [q, (q + 7) % n, (q + 13) % n, (q + 23) % n], []),
     }
-    wide = {  # CUDA-core wide-gate kernel (tensor cores off): compute-bound, reported with its FLOP rate
+    haar4 = np.linalg.qr(np.random.default_rng(4).standard_normal((16, 16))
+                         + 1j * np.random.default_rng(5).standard_normal((16, 16)))[0]
+    wide = {  # with the tensor cores off: the CUDA-core kernels (4 qubits: dense, 7: wide), with FLOP rates
+        "4q_dense_cuda_cores": lambda q, n: (haar4, [q, (q + 7) % n, (q + 13) % n, (q + 23) % n], []),
         "7q_dense_cuda_cores": lambda q, n: (haar7, [(q + 4 * i) % n for i in range(7)], []),
     }
     haar7 = np.linalg.qr(np.random.default_rng(7).standard_normal((128, 128))
@@ -428,9 +432,11 @@ def run_gates(a):
             gates = [mk(q, nq) for q in range(0, nq, 5)]
             ms, cnt, recs = timed_steps(sim, gates, 1, 1, None)
             per = [r["ms"] for r in recs if r["ms"] > 0]
-            tflops = 8.0 * 2 ** nq * 128 / (np.mean(per) * 1e-3) / 1e12 if per else 0.0
+            kq = len(gates[0][1])
+            tflops = 8.0 * 2 ** nq * 2 ** kq / (np.mean(per) * 1e-3) / 1e12 if per else 0.0
+            gbs = 2 * 2 ** nq * (8 if prec == "c64" else 16) / (np.mean(per) * 1e-3) / 1e9 if per else 0.0
             out[f"{prec}/{name}"] = {"launches": len(recs), "ms_mean": round(float(np.mean(per)), 3),
-                                     "algorithmic_tflops": round(tflops, 2)}
+                                     "algorithmic_tflops": round(tflops, 2), "frac_of_peak": round(gbs / peak, 3)}
         sim.close()
     print(json.dumps({"workload": "single-gate kernels, one pass per gate", "qubits": nq, "peak_gbs": peak,
                       "kernels": out}), flush=True)

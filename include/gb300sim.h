@@ -205,7 +205,7 @@ GSIM_API int gsim_synchronize(gsim_engine *e);
 GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
 
 /* Use (on != 0, the default) or avoid the tcgen05 tensor-core kernel for
- * fused complex64 gates of 5 to 7 targets (3xTF32 split precision). */
+ * fused complex64 gates of 4 to 7 targets (3xTF32 split precision). */
 GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int on);
 
 /* How set_wavefunction moves a host state that is already in the engine's

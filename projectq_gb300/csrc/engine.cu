@@ -918,7 +918,7 @@ class Engine {
   void exec_clusters(std::vector<StageGate> &gates, const std::vector<Cluster> &cl);
   float predict(const float *f) const;
   int dense_kind(size_t kq) const {
-    if (prec_ == GSIM_C64 && use_tc_ && kq >= 5 && kq <= 7 && N_ >= kq + 7) return 3;
+    if (prec_ == GSIM_C64 && use_tc_ && kq >= 4 && kq <= 7 && N_ >= kq + 7) return 3;
     return kq > 5 ? 2 : 0;
   }
 

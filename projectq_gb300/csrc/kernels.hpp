@@ -14,7 +14,7 @@ namespace gsim {
 
 // prec: 0 = complex128 state, 1 = complex64 state.
 cudaError_t launch_dense(int prec, void *psi, unsigned nq, const DenseOp &op, cudaStream_t s);
-// Fused dense gates of 5 to 7 targets on a complex64 state with tcgen05
+// Fused dense gates of 4 to 7 targets on a complex64 state with tcgen05
 // tensor cores (3xTF32).  d_b: the real embedding of U split into TF32 hi and
 // lo parts, laid out by tc_prepare_operand (tc_operand_floats(k) floats);
 // *d_err is set when a wait inside the kernel times out.

@@ -1,4 +1,4 @@
-// Fused dense k-qubit gates (k = 5, 6, 7) on complex64 states with the 5th
+// Fused dense k-qubit gates (k = 4 to 7) on complex64 states with the 5th
 // generation tensor cores (tcgen05, TMEM accumulators), split-precision
 // 3xTF32 with FP32 accumulation.
 //
@@ -65,7 +65,7 @@ struct TcCfg {
   static constexpr int N = K;
   static constexpr int NCH = K / kKC;
   static constexpr bool kStream = KQ >= 7;  // B streamed per chunk instead of resident
-  static constexpr int S = KQ == 5 ? 4 : (KQ == 6 ? 3 : 2);
+  static constexpr int S = KQ <= 5 ? 4 : (KQ == 6 ? 3 : 2);
   static constexpr uint32_t kStageB = kStream ? uint32_t(N) * kKC * 4u : 0u;  // one split of a B chunk
   static constexpr uint32_t kBResident = kStream ? 0u : uint32_t(N) * K * 4u;  // one split of all of B
   static constexpr uint32_t kStageBytes = 2 * kStageA + 2 * kStageB;
@@ -198,6 +198,25 @@ __device__ __forceinline__ void tmem_ld64(uint32_t taddr, float (&v)[64]) {
       : "memory");
 #pragma unroll
   for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// 32 columns (k = 4: the whole accumulator of one tile), same contract.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr)
+      : "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+template <int NC>
+__device__ __forceinline__ void tmem_ld(uint32_t taddr, float (&v)[NC]) {
+  if constexpr (NC == 64) tmem_ld64(taddr, v);
+  else tmem_ld32(taddr, v);
 }
 
 __device__ __forceinline__ uint64_t group_base(const TcArgs &A, uint64_t g) {
@@ -366,20 +385,22 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       const uint64_t g = tile * kRows + uint64_t(row);
       const bool active = g < A.groups;
       const uint64_t base = active ? group_base(A, g) : 0;
-      // 64 columns (32 outputs) per TMEM load: one wait per 64 columns
+      // EC columns (EC / 2 outputs) per TMEM load: one wait per load
+      constexpr int EC = N < 64 ? N : 64;
 #pragma unroll 1
-      for (int c0 = 0; c0 < N; c0 += 64) {
-        float v[64];
-        tmem_ld64(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+      for (int c0 = 0; c0 < N; c0 += EC) {
+        float v[EC];
+        tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
         if (active) {
           if constexpr (PAIR) {
 #pragma unroll
-            for (int q = 0; q < 32; q += 2)
+            for (int q = 0; q < EC / 2; q += 2)
               __stcs(reinterpret_cast<float4 *>(psi + base + A.off[c0 / 2 + q]),
                      make_float4(v[2 * q], v[2 * q + 1], v[2 * q + 2], v[2 * q + 3]));
           } else {
 #pragma unroll
-            for (int q = 0; q < 32; ++q) __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
+            for (int q = 0; q < EC / 2; ++q)
+              __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
           }
         }
       }
@@ -582,10 +603,11 @@ void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out) {
 
 cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
   switch (op.pos.size()) {
+    case 4: return launch_tc_k<4>(psi, nq, op, d_b, d_err, s);
     case 5: return launch_tc_k<5>(psi, nq, op, d_b, d_err, s);
     case 6: return launch_tc_k<6>(psi, nq, op, d_b, d_err, s);
     case 7: return launch_tc_k<7>(psi, nq, op, d_b, d_err, s);
-    default: throw std::invalid_argument("tensor-core gate kernel supports 5 to 7 targets");
+    default: throw std::invalid_argument("tensor-core gate kernel supports 4 to 7 targets");
   }
 }
 

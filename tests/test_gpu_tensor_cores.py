@@ -1,4 +1,4 @@
-"""Fused 5-, 6- and 7-qubit gates on complex64 states through the tcgen05
+"""Fused 4- to 7-qubit gates on complex64 states through the tcgen05
 tensor-core kernel (3xTF32, FP32 accumulation), against the complex128 path
 (FP64 arithmetic) and against complex64 on CUDA cores.  The gates are
 Haar-random with targets spanning low and high bit positions, with and
@@ -27,7 +27,8 @@ def run(prec, tc, n, psi, gates):
     return s.cheat()[1]
 
 
-@pytest.mark.parametrize("k,n", [(5, 13), (5, 15), (6, 15), (7, 15), (5, 24), (6, 23), (7, 22)])
+@pytest.mark.parametrize("k,n", [(4, 12), (4, 16), (4, 24), (5, 13), (5, 15), (6, 15), (7, 15), (5, 24), (6, 23),
+                                 (7, 22)])
 def test_tensor_core_gates_match_fp64(k, n):
     rng = np.random.default_rng(40 + k + n)
     psi = random_state(n, seed=k)
