@@ -500,11 +500,10 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
   A.ntiles = uint64_t(1) << (nq - plan.L);
   for (size_t i = 0; i < plan.lpos.size(); ++i) A.lpos[i] = uint8_t(plan.lpos[i]);
   const size_t smem = (size_t(1) << A.L) * sizeof(cplx_t<T>) + (size_t(1) << A.h) * 8;
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaFuncSetAttribute(stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
-    attr_set = true;
-  }
+  // set on every launch: attributes belong to the current device, and the
+  // call is cheap next to a pass over the state
+  cudaError_t ae = cudaFuncSetAttribute(stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
+  if (ae != cudaSuccess) return ae;
   if (!plan.subs.empty()) {
     // Register substages: d_ops holds the table [SubstageDev...][SubOpDev...][pool].
     constexpr int R = sizeof(T) == 4 ? int(kRegBitsC64) : int(kRegBitsC128);
@@ -520,11 +519,8 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
     const size_t smem_reg = (size_t(1) << A.L) * sizeof(cplx_t<T>) + (((size_t(1) << A.h) * 8 + 15) & ~size_t(15)) +
                             pool_bytes;
     if (smem_reg > 200 * 1024) return cudaErrorInvalidValue;
-    static bool reg_attr = false;
-    if (!reg_attr) {
-      cudaFuncSetAttribute(stage_reg_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-      reg_attr = true;
-    }
+    ae = cudaFuncSetAttribute(stage_reg_kernel<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (ae != cudaSuccess) return ae;
     int per_sm = 1;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_reg_kernel<T, R>, 256, smem_reg);
     per_sm = std::max(1, per_sm);

@@ -512,13 +512,10 @@ cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float 
     for (int l = 0; l < KQ; ++l)
       if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
   A.groups = uint64_t(1) << (nq - ins.size());
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gate_kernel<KQ, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         int(Cfg::kSmem));
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  // set on every launch: attributes belong to the current device
+  const cudaError_t e =
+      cudaFuncSetAttribute(tc_gate_kernel<KQ, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::kSmem));
+  if (e != cudaSuccess) return e;
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
