@@ -357,6 +357,11 @@ def run_fused(a):
         sim.allocate_qubit(q)
     ms, cnt, recs = timed_steps(sim, gates, a.steps, a.warmup, None)
     key, groups = dominant_kernel(recs)
+    # the same gates without the per-group norm restoration (tensor-core mode 2)
+    sim.set_tensor_cores(True, renorm=False)
+    ms_nr, _, recs_nr = timed_steps(sim, gates, a.steps, 1, None)
+    _, groups_nr = dominant_kernel(recs_nr)
+    sim.set_tensor_cores(True)
     flops = sum(8.0 * 2 ** nq * 2 ** len(t) for _, t, _ in gates) * a.steps
     # accuracy at 24 qubits against complex128 (FP64 arithmetic)
     small = gates_for(24, 30, 1)
@@ -384,6 +389,9 @@ def run_fused(a):
                       "hbm_gbs": cnt["gate_bytes"] / (ms * 1e-3) / 1e9,
                       "accuracy_24q_30gates": {"one_minus_fidelity": 1 - abs(ip) ** 2 / (n1 * n2), "max_abs_err": maxerr},
                       "accuracy_sampled_full_width": sampled,
+                      "without_norm_restoration": {
+                          "ms_per_step": ms_nr / a.steps,
+                          "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups_nr.items()}},
                       "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
 
 

@@ -690,9 +690,13 @@ class Engine {
     if (mode != 0 && mode != 1) fail(GSIM_ERR_VALUE, "upload mode must be 0 (copy engine) or 1 (SM reads)");
     upload_mode_ = mode;
   }
-  void set_tensor_cores(bool on) {
+  // 0 off, 1 on with the per-group norm restoration of unitary gates
+  // (default), 2 on without it
+  void set_tensor_cores(int mode) {
     run();
-    use_tc_ = on;
+    if (mode < 0 || mode > 2) fail(GSIM_ERR_VALUE, "tensor-core mode must be 0, 1 or 2");
+    use_tc_ = mode != 0;
+    tc_mode_ = mode == 0 ? 1 : mode;
   }
 
   // ---- timing -------------------------------------------------------------
@@ -815,7 +819,7 @@ class Engine {
       const void *d = finish_slot(sl, h, nb);
       int *d_err = reinterpret_cast<int *>(static_cast<char *>(small_.get(4096)) + 2048);
       if (!tc_used_) CK(cudaMemsetAsync(d_err, 0, sizeof(int), stream_));
-      CK(launch_tc_gate(state_.p, N_, sop, static_cast<const float *>(d), d_err, stream_));
+      CK(launch_tc_gate(state_.p, N_, sop, static_cast<const float *>(d), d_err, tc_mode_ == 1, stream_));
       tc_used_ = true;
     } else if (route == 2) {
       const size_t D = size_t(1) << op.pos.size();
@@ -1037,6 +1041,7 @@ class Engine {
   unsigned tile_bits_c64_ = kRegBitsC64 + 8, tile_bits_c128_ = kRegBitsC128 + 8;
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
+  int tc_mode_ = 1;
   int upload_mode_ = 1;  // host -> device state copies: 0 copy engine, 1 SM reads of page-locked memory
   bool tc_used_ = false;
   std::array<UploadSlot, 4> mslots_;
@@ -2021,7 +2026,7 @@ int gsim_set_upload_mode(gsim_engine *e, int mode) {
   return guard([&] { E(e)->set_upload_mode(mode); });
 }
 int gsim_set_tensor_cores(gsim_engine *e, int on) {
-  return guard([&] { E(e)->set_tensor_cores(on != 0); });
+  return guard([&] { E(e)->set_tensor_cores(on); });
 }
 int gsim_set_device(int device) {
   return guard([&] { CK(cudaSetDevice(device)); });

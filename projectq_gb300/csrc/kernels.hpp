@@ -23,7 +23,10 @@ size_t tc_operand_floats(int k);
 // kernel loads and stores adjacent amplitude pairs when a target is bit 0.
 DenseOp tc_sorted_targets(const DenseOp &op);
 void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out);
-cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s);
+// renorm: when U is unitary, rescale each amplitude group's outputs to the
+// group's input norm (undoes the tensor cores' downward accumulation bias).
+cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, bool renorm,
+                           cudaStream_t s);
 // Gates of 5 to 7 targets on CUDA cores; d_matrix: the 2^k x 2^k matrix
 // TRANSPOSED (column j contiguous: element [j][r] = U[r][j]) in the state's
 // precision in device memory.

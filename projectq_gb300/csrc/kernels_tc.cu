@@ -70,7 +70,10 @@ struct TcCfg {
   static constexpr uint32_t kBResident = kStream ? 0u : uint32_t(N) * K * 4u;  // one split of all of B
   static constexpr uint32_t kStageBytes = 2 * kStageA + 2 * kStageB;
   static constexpr uint32_t kBarOff = 2 * kBResident + S * kStageBytes;
-  static constexpr uint32_t kSmem = kBarOff + 256;
+  // input norms handed from the producers to the epilogue: float [NB][kRows][2 halves]
+  static constexpr int NB = KQ == 6 ? 2 : 4;
+  static constexpr uint32_t kNormOff = kBarOff + 256;
+  static constexpr uint32_t kSmem = kNormOff + uint32_t(NB) * kRows * 2 * 4;
   static constexpr int kThreads = kStream ? 448 : 416;
   static constexpr uint32_t kTmemCols = 2u * N < 32u ? 32u : 2u * N;
 };
@@ -79,6 +82,7 @@ struct TcArgs {
   uint64_t groups;      // number of amplitude groups
   uint64_t ctrl_set;
   int nins, k;
+  int renorm;           // U is unitary: rescale each group's outputs to its input norm
   uint8_t ins[64];
   uint64_t off[128];    // offset of amplitude j of a group (j < 2^k, k <= 7)
 };
@@ -278,13 +282,15 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
   unsigned char *bres = sm;                             // resident B: hi then lo (k <= 6)
   unsigned char *stages = sm + 2 * Cfg::kBResident;    // S x [A hi | A lo | B hi | B lo]
   uint64_t *bars = reinterpret_cast<uint64_t *>(sm + Cfg::kBarOff);
-  // bars: full[S], empty[S], accf[2], acce[2], drain
+  // bars: full[S], empty[S], accf[2], acce[2], drain, (abort flag), (TMEM slot), nfull[NB], nemp[NB]
   volatile int *abort_flag = reinterpret_cast<volatile int *>(bars + 2 * S + 5);
   uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(bars + 2 * S + 6);
+  float *nin = reinterpret_cast<float *>(sm + Cfg::kNormOff);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const uint32_t full0 = smem_u32(bars), empty0 = smem_u32(bars + S), accf0 = smem_u32(bars + 2 * S),
-                 acce0 = smem_u32(bars + 2 * S + 2), drain = smem_u32(bars + 2 * S + 4);
+                 acce0 = smem_u32(bars + 2 * S + 2), drain = smem_u32(bars + 2 * S + 4),
+                 nfull0 = smem_u32(bars + 2 * S + 7), nemp0 = smem_u32(bars + 2 * S + 7 + Cfg::NB);
 
   if constexpr (!Cfg::kStream) {
     const uint4 *src = reinterpret_cast<const uint4 *>(bsrc);
@@ -302,6 +308,10 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       mbar_init(acce0 + 8 * b, kEpilogue);
     }
     mbar_init(drain, 1);
+    for (int b = 0; b < Cfg::NB; ++b) {
+      mbar_init(nfull0 + 8 * b, kProducers);
+      mbar_init(nemp0 + 8 * b, kEpilogue);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 0) {
@@ -348,6 +358,7 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       }
     };
     uint64_t it = 0;
+    float nacc = 0.f;  // this thread's share of its group's input norm (renorm)
     auto publish = [&](const float2 (&x)[8]) -> bool {
       const int s = int(it % S);
       const uint32_t u = uint32_t(it / S);
@@ -355,6 +366,17 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       split_store(stages + size_t(s) * Cfg::kStageBytes, row, half, x);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full0 + 8 * s);
+      if (A.renorm) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) nacc = fmaf(x[q].x, x[q].x, fmaf(x[q].y, x[q].y, nacc));
+        if (int(it % NCH) == NCH - 1) {  // the tile's last chunk: hand the norm to the epilogue
+          const uint32_t ti = uint32_t(it / NCH), b = ti % Cfg::NB, ub = ti / Cfg::NB;
+          if (ub > 0 && !mbar_wait(nemp0 + 8 * b, (ub - 1) & 1u, abort_flag, err)) return false;
+          nin[(b * kRows + row) * 2 + half] = nacc;
+          mbar_arrive(nfull0 + 8 * b);
+          nacc = 0.f;
+        }
+      }
       ++it;
       return true;
     };
@@ -387,10 +409,32 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       const uint64_t base = active ? group_base(A, g) : 0;
       // EC columns (EC / 2 outputs) per TMEM load: one wait per load
       constexpr int EC = N < 64 ? N : 64;
+      // The tensor cores' FP32 accumulation shrinks sums slightly (measured
+      // 1e-8 x K relative per gate, always downwards), which for a unitary U
+      // is a loss of norm; each group's outputs are rescaled to the group's
+      // input norm (exact for unitary U up to FP32 rounding).
+      float scale = 1.f;
+      if (A.renorm) {
+        const uint32_t nb = i % Cfg::NB, nu = i / Cfg::NB;
+        if (!mbar_wait(nfull0 + 8 * nb, nu & 1u, abort_flag, err)) break;
+        const float s_in = nin[(nb * kRows + row) * 2] + nin[(nb * kRows + row) * 2 + 1];
+        mbar_arrive(nemp0 + 8 * nb);
+        float s_out = 0.f;
+#pragma unroll 1
+        for (int c0 = 0; c0 < N; c0 += EC) {
+          float v[EC];
+          tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+#pragma unroll
+          for (int q = 0; q < EC; ++q) s_out = fmaf(v[q], v[q], s_out);
+        }
+        if (s_out > 0.f && s_in > 0.f) scale = sqrtf(s_in / s_out);
+      }
 #pragma unroll 1
       for (int c0 = 0; c0 < N; c0 += EC) {
         float v[EC];
         tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+#pragma unroll
+        for (int q = 0; q < EC; ++q) v[q] *= scale;
         if (active) {
           if constexpr (PAIR) {
 #pragma unroll
@@ -494,8 +538,35 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
                  : "memory");
 }
 
+// U unitary (to 1e-10): the norms of two fixed pseudo-random vectors are kept.
+bool tc_is_unitary(const std::vector<cplx> &U, int k) {
+  const size_t D = size_t(1) << k;
+  uint64_t st = 0x9E3779B97F4A7C15ull;
+  for (int trial = 0; trial < 2; ++trial) {
+    std::vector<cplx> v(D);
+    double nv = 0;
+    for (size_t j = 0; j < D; ++j) {
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      const double re = double(int64_t(st >> 11) % 1000003) / 1000003.0 - 0.5;
+      st = st * 6364136223846793005ull + 1442695040888963407ull;
+      const double im = double(int64_t(st >> 11) % 1000003) / 1000003.0 - 0.5;
+      v[j] = cplx(re, im);
+      nv += re * re + im * im;
+    }
+    double nw = 0;
+    for (size_t a = 0; a < D; ++a) {
+      cplx w = 0;
+      for (size_t j = 0; j < D; ++j) w += U[a * D + j] * v[j];
+      nw += std::norm(w);
+    }
+    if (!(std::abs(nw - nv) <= 1e-10 * nv)) return false;
+  }
+  return true;
+}
+
 template <int KQ, bool PAIR>
-cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
+cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, bool renorm,
+                         cudaStream_t s) {
   using Cfg = TcCfg<KQ>;
   TcArgs A;
   std::memset(&A, 0, sizeof(A));
@@ -512,6 +583,7 @@ cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float 
     for (int l = 0; l < KQ; ++l)
       if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
   A.groups = uint64_t(1) << (nq - ins.size());
+  A.renorm = renorm && tc_is_unitary(op.m, KQ) ? 1 : 0;
   // set on every launch: attributes belong to the current device
   const cudaError_t e =
       cudaFuncSetAttribute(tc_gate_kernel<KQ, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::kSmem));
@@ -526,9 +598,10 @@ cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float 
 }
 
 template <int KQ>
-cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
-  if (op.pos[0] == 0) return launch_tc_kp<KQ, true>(psi, nq, op, d_b, d_err, s);
-  return launch_tc_kp<KQ, false>(psi, nq, op, d_b, d_err, s);
+cudaError_t launch_tc_k(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, bool renorm,
+                        cudaStream_t s) {
+  if (op.pos[0] == 0) return launch_tc_kp<KQ, true>(psi, nq, op, d_b, d_err, renorm, s);
+  return launch_tc_kp<KQ, false>(psi, nq, op, d_b, d_err, renorm, s);
 }
 
 }  // namespace
@@ -598,12 +671,13 @@ void tc_prepare_operand(const std::vector<cplx> &U, int k, float *out) {
     }
 }
 
-cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, cudaStream_t s) {
+cudaError_t launch_tc_gate(void *psi, unsigned nq, const DenseOp &op, const float *d_b, int *d_err, bool renorm,
+                           cudaStream_t s) {
   switch (op.pos.size()) {
-    case 4: return launch_tc_k<4>(psi, nq, op, d_b, d_err, s);
-    case 5: return launch_tc_k<5>(psi, nq, op, d_b, d_err, s);
-    case 6: return launch_tc_k<6>(psi, nq, op, d_b, d_err, s);
-    case 7: return launch_tc_k<7>(psi, nq, op, d_b, d_err, s);
+    case 4: return launch_tc_k<4>(psi, nq, op, d_b, d_err, renorm, s);
+    case 5: return launch_tc_k<5>(psi, nq, op, d_b, d_err, renorm, s);
+    case 6: return launch_tc_k<6>(psi, nq, op, d_b, d_err, renorm, s);
+    case 7: return launch_tc_k<7>(psi, nq, op, d_b, d_err, renorm, s);
     default: throw std::invalid_argument("tensor-core gate kernel supports 4 to 7 targets");
   }
 }

@@ -363,9 +363,10 @@ class Simulator:
     def set_fusion(self, mode="reference", kmax=0):
         self._check(self._api.set_fusion(self._h, _FUSION[mode], int(kmax)))
 
-    def set_tensor_cores(self, on=True):
-        """Use tcgen05 tensor cores for fused complex64 gates of 5-6 targets."""
-        self._check(self._api.set_tensor_cores(self._h, 1 if on else 0))
+    def set_tensor_cores(self, on=True, renorm=True):
+        """Use tcgen05 tensor cores for fused complex64 gates of 4-7 targets;
+        renorm restores each amplitude group's norm after a unitary gate."""
+        self._check(self._api.set_tensor_cores(self._h, (1 if renorm else 2) if on else 0))
 
     def synchronize(self):
         self._check(self._api.synchronize(self._h))

@@ -50,3 +50,30 @@ def test_tensor_core_gates_match_fp64(k, n):
     assert err < 5e-6, err
     assert 1 - fid < 1e-10, 1 - fid
     assert np.max(np.abs(cuda - ref)) < 5e-6
+
+
+def test_norm_restoration_of_unitary_gates():
+    """The tensor cores' FP32 accumulation loses norm systematically (about
+    1e-8 x 2^(k+1) per gate); the default mode restores each amplitude
+    group's input norm after a unitary gate.  200 alternating U, U^dagger
+    7-qubit gates: the norm drifts at least 5x less with the restoration, and
+    the state returns to the start within 1 - F 1e-7 either way."""
+    n = 16
+    psi = random_state(n, seed=1)
+    U = haar_unitary(7, np.random.default_rng(7))
+    targets = [0, 3, 7, 11, 13, 14, 15]
+    drift = {}
+    for renorm in (True, False):
+        s = make("gpu", seed=1, precision="c64", fusion="none")
+        allocate(s, n)
+        s.set_tensor_cores(True, renorm=renorm)
+        s.set_wavefunction(psi, list(range(n)))
+        for it in range(200):
+            s.apply_controlled_gate(U if it % 2 == 0 else U.conj().T, targets, [])
+        s.run()
+        v = s.cheat()[1]
+        nv = float(np.vdot(v, v).real)
+        drift[renorm] = abs(1 - nv)
+        assert 1 - abs(np.vdot(psi, v)) ** 2 / nv < 1e-7
+    assert drift[True] < 3e-5, drift
+    assert drift[True] * 5 < drift[False], drift
