@@ -205,11 +205,11 @@ GSIM_API int gsim_synchronize(gsim_engine *e);
 GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
 
 /* The tcgen05 tensor-core kernel for fused complex64 gates of 4 to 7 targets
- * (3xTF32 split precision): on = 0 off (CUDA cores), 1 on (default) with the
+ * (3xTF32 split precision): mode 0 off (CUDA cores), 1 on (default) with the
  * norm of every amplitude group restored after a unitary gate (the tensor
  * cores' FP32 accumulation otherwise loses about 1e-8 x 2^(k+1) of the norm
  * per gate), 2 on without that restoration. */
-GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int on);
+GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int mode);
 
 /* How set_wavefunction moves a host state that is already in the engine's
  * precision: 1 (default) the SMs read it through the device view of

@@ -2025,8 +2025,8 @@ int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms) {
 int gsim_set_upload_mode(gsim_engine *e, int mode) {
   return guard([&] { E(e)->set_upload_mode(mode); });
 }
-int gsim_set_tensor_cores(gsim_engine *e, int on) {
-  return guard([&] { E(e)->set_tensor_cores(on); });
+int gsim_set_tensor_cores(gsim_engine *e, int mode) {
+  return guard([&] { E(e)->set_tensor_cores(mode); });
 }
 int gsim_set_device(int device) {
   return guard([&] { CK(cudaSetDevice(device)); });
