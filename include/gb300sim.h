@@ -159,7 +159,11 @@ GSIM_API int gsim_apply_qubit_operator(gsim_engine *e, const uint32_t *term_offs
                               const double *coeffs, size_t nterms, const uint32_t *ids,
                               size_t nids);
 
-/* emulate_time_evolution — simulator.hpp:386-438.  Real coefficients. */
+/* emulate_time_evolution — simulator.hpp:386-438.  Real coefficients.
+ * By default, when every pair of non-identity terms commutes and no term acts
+ * on a control, exp(-i t H) is applied exactly as the product of the terms'
+ * exponentials (one gate per term, fused by the planner); otherwise by the
+ * reference's Taylor series (see gsim_set_time_evolution). */
 GSIM_API int gsim_emulate_time_evolution(gsim_engine *e, const uint32_t *term_offsets,
                                 const uint32_t *op_qubit, const uint8_t *op_pauli,
                                 const double *coeffs, size_t nterms, double time,
@@ -211,6 +215,14 @@ GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
  * per gate), 2 on without that restoration. */
 GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int mode);
 
+/* How emulate_time_evolution evaluates exp(-i t H): mode 1 (default) exactly,
+ * as the product of exp(-i t c_k P_k) over the terms, when they commute
+ * pairwise and none acts on a control (the commuting case that ProjectQ's
+ * setups/decompositions/time_evolution.py:28-52 decomposes), else as mode 0;
+ * mode 0 always by the Taylor series of simulator.hpp:386-438 (the two agree to
+ * the series' truncation, about 1e-12). */
+GSIM_API int gsim_set_time_evolution(gsim_engine *e, int mode);
+
 /* How set_wavefunction moves a host state that is already in the engine's
  * precision: 1 (default) the SMs read it through the device view of
  * page-locked host memory (gsim_host_register / cudaMallocHost, 16-byte
@@ -226,7 +238,9 @@ GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
 /* Counters since creation or the last reset:
  *  out[0] logical gates submitted, out[1] kernel launches for gates,
  *  out[2] algorithmic bytes moved by gate kernels (2 x touched amplitudes
- *  x bytes per amplitude), out[3] gate passes over the state. */
+ *  x bytes per amplitude), out[3] gate passes over the state, out[4] time
+ *  evolutions applied as a product of term exponentials, out[5] time
+ *  evolutions by the Taylor series. */
 GSIM_API int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n);
 GSIM_API int gsim_reset_counters(gsim_engine *e);
 

@@ -229,6 +229,10 @@ class Engine {
         fail(GSIM_ERR_VALUE, "apply_controlled_gate(): a control is also a target or repeated");
     }
     counters_[0] += 1;
+    submit_gate(std::move(m), ids, ctrl);
+  }
+  // Queue (or fuse, or run) a validated gate under the current fusion mode.
+  void submit_gate(std::vector<cplx> m, const std::vector<unsigned> &ids, const std::vector<unsigned> &ctrl) {
     if (mode_ == GSIM_FUSION_STAGED || mode_ == GSIM_FUSION_LEARNED) {
       queue_.push_back(QueuedGate{std::move(m), ids, ctrl});
       if (queue_.size() >= kMaxQueue) run();
@@ -405,12 +409,103 @@ class Engine {
     CK(cudaStreamSynchronize(stream_));
   }
 
+  // exp(-i t H) for H = sum_k c_k P_k whose terms commute pairwise, as the
+  // exact product of exp(-i t c_k P_k) = cos(t c_k) I - i sin(t c_k) P_k --
+  // what ProjectQ's commuting-terms decomposition
+  // (setups/decompositions/time_evolution.py:28-52) expresses in gates --
+  // without the Taylor series.  A term on at most kTermGateQubits qubits
+  // becomes one controlled gate on its support, queued for the planner, so
+  // many terms share a pass over the state (ZZ and Z terms are diagonal gates);
+  // a wider term is one pass of the rotation kernel.  The identity terms'
+  // phase exp(-i t tr) goes into the first exponential.  Returns false (and
+  // does nothing) unless every term commutes with every other and none acts
+  // on a control qubit.
+  static constexpr unsigned kTermGateQubits = 5;
+  bool evolve_commuting(const std::vector<PauliTerm> &terms, const std::vector<double> &coeffs,
+                        double time, const std::vector<unsigned> &ctrl, uint64_t cm) {
+    std::vector<size_t> ks;
+    double tr = 0.;
+    for (size_t t = 0; t < terms.size(); ++t) {
+      if (terms[t].empty) {
+        tr += coeffs[t];
+        continue;
+      }
+      if ((terms[t].xmask | terms[t].sign_mask) & cm) return false;
+      ks.push_back(t);
+    }
+    if (ks.empty()) return false;
+    for (size_t a = 0; a < ks.size(); ++a)
+      for (size_t b = a + 1; b < ks.size(); ++b) {
+        const PauliTerm &p = terms[ks[a]], &q = terms[ks[b]];
+        if ((__builtin_popcountll(p.xmask & q.sign_mask) + __builtin_popcountll(p.sign_mask & q.xmask)) & 1)
+          return false;
+      }
+    std::vector<unsigned> id_at(N_, 0);
+    for (auto const &kv : map_) id_at[kv.second] = kv.first;
+    static const cplx ph[4] = {cplx(1, 0), cplx(0, -1), cplx(-1, 0), cplx(0, 1)};  // (-i)^ny
+    cplx g = std::exp(cplx(0., -time * tr));
+    for (size_t k : ks) {
+      const PauliTerm &p = terms[k];
+      const double th = time * coeffs[k];
+      const cplx a = g * std::cos(th), b = g * cplx(0., -std::sin(th)) * ph[p.ny & 3];
+      g = 1.;
+      const uint64_t supp = p.xmask | p.sign_mask;
+      const unsigned w = unsigned(__builtin_popcountll(supp));
+      if (w <= kTermGateQubits) {
+        // the gate on the support, local bit i = i-th lowest support position:
+        // M = a I + b X^x Z^z with (X^x Z^z)[r][r ^ x] = (-1)^{popcount(r & z)}
+        std::vector<unsigned> ids, at;
+        for (unsigned q = 0; q < N_; ++q)
+          if ((supp >> q) & 1) {
+            ids.push_back(id_at[q]);
+            at.push_back(q);
+          }
+        uint32_t lx = 0, lz = 0;
+        for (unsigned i = 0; i < w; ++i) {
+          lx |= uint32_t((p.xmask >> at[i]) & 1) << i;
+          lz |= uint32_t((p.sign_mask >> at[i]) & 1) << i;
+        }
+        const size_t d = size_t(1) << w;
+        std::vector<cplx> m(d * d, cplx(0., 0.));
+        for (size_t r = 0; r < d; ++r) {
+          m[r * d + r] += a;
+          m[r * d + (r ^ lx)] += (__builtin_popcount(uint32_t(r) & lz) & 1) ? -b : b;
+        }
+        submit_gate(std::move(m), ids, ctrl);
+      } else {
+        run();
+        PauliRotationDev rd{};
+        rd.xmask = p.xmask;
+        rd.zmask = p.sign_mask;
+        rd.ctrl = cm;
+        rd.are = a.real();
+        rd.aim = a.imag();
+        rd.bre = b.real();
+        rd.bim = b.imag();
+        const uint64_t piv = p.xmask & (~p.xmask + 1);
+        const uint64_t ins = piv | cm;
+        for (unsigned q = 0; q < N_; ++q)
+          if ((ins >> q) & 1) rd.pos[rd.npos++] = uint8_t(q);
+        CK(launch_pauli_rotation(prec_, state_.p, N_, rd, stream_));
+        const uint64_t bytes = 2 * (uint64_t(1) << (N_ - unsigned(__builtin_popcountll(cm)))) * bpa_;
+        counters_[1] += 1;
+        counters_[2] += bytes;
+        counters_[3] += 1;
+      }
+    }
+    run();
+    counters_[4] += 1;
+    return true;
+  }
+
   // ---- simulator.hpp:386-438 ----------------------------------------------
   void emulate_time_evolution(const std::vector<PauliTerm> &terms, const std::vector<double> &coeffs,
                               double time, const std::vector<unsigned> &ctrl) {
     run();
     uint64_t cm = 0;
     for (unsigned c : ctrl) cm |= uint64_t(1) << pos_of(c);
+    if (te_mode_ == 1 && evolve_commuting(terms, coeffs, time, ctrl, cm)) return;
+    counters_[5] += 1;
     double tr = 0., op_nrm = 0.;
     std::vector<PauliApplyTermDev> dev;
     for (size_t t = 0; t < terms.size(); ++t) {
@@ -421,6 +516,9 @@ class Engine {
         op_nrm += std::abs(coeffs[t]);
       }
     }
+    // group terms that share a flip mask (one gather per group in the kernel)
+    std::stable_sort(dev.begin(), dev.end(),
+                     [](const PauliApplyTermDev &a, const PauliApplyTermDev &b) { return a.xmask < b.xmask; });
     const unsigned s = unsigned(std::abs(time) * op_nrm + 1.);
     const cplx I(0., 1.);
     const cplx corr = std::exp(-time * I * tr / double(s));
@@ -699,6 +797,11 @@ class Engine {
     tc_mode_ = mode == 0 ? 1 : mode;
   }
 
+  void set_time_evolution(int mode) {
+    if (mode != 0 && mode != 1) fail(GSIM_ERR_VALUE, "time-evolution mode must be 0 (Taylor series) or 1 (exact for commuting terms)");
+    te_mode_ = mode;
+  }
+
   // ---- timing -------------------------------------------------------------
   void timer_mark(int slot) {
     if (slot < 0 || slot >= 16) fail(GSIM_ERR_VALUE, "timer slot must be 0..15");
@@ -733,7 +836,7 @@ class Engine {
     prof_.clear();
     ev_next_ = 0;
   }
-  uint64_t counter(size_t i) const { return i < 4 ? counters_[i] : 0; }
+  uint64_t counter(size_t i) const { return i < 6 ? counters_[i] : 0; }
   void reset_counters() { std::fill(std::begin(counters_), std::end(counters_), 0); }
 
  private:
@@ -1042,6 +1145,7 @@ class Engine {
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
   int tc_mode_ = 1;
+  int te_mode_ = 1;  // emulate_time_evolution: 0 Taylor series only, 1 exact product for commuting terms
   int upload_mode_ = 1;  // host -> device state copies: 0 copy engine, 1 SM reads of page-locked memory
   bool tc_used_ = false;
   std::array<UploadSlot, 4> mslots_;
@@ -1055,7 +1159,7 @@ class Engine {
   DevBuf upload_dev_;
   HostBuf upload_host_;
   cudaEvent_t upload_ev_ = nullptr;
-  uint64_t counters_[4] = {0, 0, 0, 0};
+  uint64_t counters_[6] = {0, 0, 0, 0, 0, 0};
   // timing
   cudaEvent_t timer_[16] = {};
   struct Prof {
@@ -2027,6 +2131,9 @@ int gsim_set_upload_mode(gsim_engine *e, int mode) {
 }
 int gsim_set_tensor_cores(gsim_engine *e, int mode) {
   return guard([&] { E(e)->set_tensor_cores(mode); });
+}
+int gsim_set_time_evolution(gsim_engine *e, int mode) {
+  return guard([&] { E(e)->set_time_evolution(mode); });
 }
 int gsim_set_device(int device) {
   return guard([&] { CK(cudaSetDevice(device)); });

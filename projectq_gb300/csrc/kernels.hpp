@@ -110,6 +110,21 @@ cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *o
 cudaError_t launch_phase_ctrl(double2 *out, double2 *vec, uint64_t n, uint64_t ctrl, double cre,
                               double cim, cudaStream_t s);
 
+// One Pauli exponential in place, on the amplitudes whose control bits are
+// all set:  psi <- a psi + b P psi, with (P psi)_j = (-1)^{popcount(j & z)}
+// psi_{j ^ x} (the term's own phase folded into b by the host).  For
+// exp(-i theta c P') with P' = phase X^x Z^z: a = g cos(theta), b =
+// -i g sin(theta) phase, g an optional global phase.  x and z must not meet
+// ctrl.  One read and one write of every controlled amplitude.
+struct PauliRotationDev {
+  uint64_t xmask, zmask, ctrl;
+  double are, aim, bre, bim;
+  uint8_t pos[64];  // pivot (lowest bit of x, if any) and control positions, ascending
+  int npos;
+};
+cudaError_t launch_pauli_rotation(int prec, void *psi, unsigned nq, const PauliRotationDev &r,
+                                  cudaStream_t s);
+
 // emulate_math: out_j = sum over sources s of in_s, gathered through an
 // inverse table (CSR) over the packed register value, in the reference's
 // accumulation order; uncontrolled indices are copied.

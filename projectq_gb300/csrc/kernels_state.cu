@@ -379,9 +379,15 @@ __global__ void __launch_bounds__(256) taylor_step_kernel(
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
     double ur = 0., ui = 0.;
+    // terms arrive grouped by flip mask: one gather per group
+    uint64_t xprev = ~uint64_t(0);
+    double2 v = make_double2(0., 0.);
     for (int t = 0; t < nterms; ++t) {
       const PauliApplyTermDev pt = terms[t];
-      const double2 v = vec[j ^ pt.xmask];
+      if (pt.xmask != xprev) {
+        v = vec[j ^ pt.xmask];
+        xprev = pt.xmask;
+      }
       const bool neg = __popcll(j & pt.sign_mask) & 1;
       // (P_t vec)_j = phase * sign * vec[j ^ x], exact; times the real c_t.
       // pt.cre/pt.cim hold (-i)^{#Y} and pt.sign_mask the Y|Z positions;
@@ -408,6 +414,33 @@ __global__ void __launch_bounds__(256) taylor_step_kernel(
   }
   const double s = block_sum(nrm);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// psi <- a psi + b P psi over the controlled subspace.  With x != 0 a thread
+// owns the pair (j, j ^ x), j with the pivot bit clear, and writes both; with
+// x == 0 the map is diagonal, one amplitude per index.
+template <typename T>
+__global__ void __launch_bounds__(256) pauli_rotation_kernel(cplx_t<T> *__restrict__ psi, uint64_t units,
+                                                             const __grid_constant__ PauliRotationDev r) {
+  const T are = T(r.are), aim = T(r.aim), bre = T(r.bre), bim = T(r.bim);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < units; u += stride) {
+    const uint64_t j = insert_zeros(u, r.pos, r.npos) | r.ctrl;
+    const cplx_t<T> p = psi[j];
+    const T sj = (__popcll(j & r.zmask) & 1) ? T(-1) : T(1);
+    if (r.xmask == 0) {
+      const T fr = are + sj * bre, fi = aim + sj * bim;
+      psi[j] = mkc<T>(fr * p.x - fi * p.y, fr * p.y + fi * p.x);
+      continue;
+    }
+    const uint64_t k = j ^ r.xmask;
+    const cplx_t<T> q = psi[k];
+    const T sk = (__popcll(k & r.zmask) & 1) ? T(-1) : T(1);
+    // new p = a p + sj b q ; new q = a q + sk b p
+    const T cr = sj * bre, ci = sj * bim, dr = sk * bre, di = sk * bim;
+    psi[j] = mkc<T>(are * p.x - aim * p.y + cr * q.x - ci * q.y, are * p.y + aim * p.x + cr * q.y + ci * q.x);
+    psi[k] = mkc<T>(are * q.x - aim * q.y + dr * p.x - di * p.y, are * q.y + aim * q.x + dr * p.y + di * p.x);
+  }
 }
 
 __global__ void phase_ctrl_kernel(double2 *__restrict__ out, double2 *__restrict__ vec, uint64_t n,
@@ -703,6 +736,17 @@ cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *o
 cudaError_t launch_phase_ctrl(double2 *out, double2 *vec, uint64_t n, uint64_t ctrl, double cre,
                               double cim, cudaStream_t s) {
   phase_ctrl_kernel<<<grid(n, 256), 256, 0, s>>>(out, vec, n, ctrl, cre, cim);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pauli_rotation(int prec, void *psi, unsigned nq, const PauliRotationDev &r,
+                                  cudaStream_t s) {
+  if (r.npos < 0 || unsigned(r.npos) > nq) return cudaErrorInvalidValue;
+  const uint64_t units = uint64_t(1) << (nq - unsigned(r.npos));
+  if (prec == 1)
+    pauli_rotation_kernel<float><<<grid(units, 256), 256, 0, s>>>(static_cast<float2 *>(psi), units, r);
+  else
+    pauli_rotation_kernel<double><<<grid(units, 256), 256, 0, s>>>(static_cast<double2 *>(psi), units, r);
   return cudaGetLastError();
 }
 

@@ -285,7 +285,9 @@ class Simulator:
                                                    _p(ida, C.c_uint32), len(ida)))
 
     def emulate_time_evolution(self, terms, time, ids, ctrl):
-        """simulator.hpp:386-438: exp(-i t H) by Taylor series (FP64)."""
+        """simulator.hpp:386-438: exp(-i t H); exactly as a product of term
+        exponentials when the terms commute (set_time_evolution), else by the
+        Taylor series (FP64)."""
         off, q, pa, cs = _pauli_csr(terms, real=True)
         ida = _u32(_ids(ids))
         ctrl = _u32(_ids(ctrl))
@@ -368,6 +370,15 @@ class Simulator:
         renorm restores each amplitude group's norm after a unitary gate."""
         self._check(self._api.set_tensor_cores(self._h, (1 if renorm else 2) if on else 0))
 
+    def set_time_evolution(self, mode="exact"):
+        """emulate_time_evolution: "exact" (default: the product of the terms'
+        exponentials when they commute pairwise and avoid the controls, else the
+        Taylor series) or "taylor" (always the reference's Taylor series)."""
+        modes = {"taylor": 0, "exact": 1}
+        if mode not in modes:
+            raise ValueError(f"time-evolution mode must be one of {sorted(modes)}")
+        self._check(self._api.set_time_evolution(self._h, modes[mode]))
+
     def synchronize(self):
         self._check(self._api.synchronize(self._h))
 
@@ -381,10 +392,10 @@ class Simulator:
         self._check(self._api.reserve(self._h, int(nqubits)))
 
     def counters(self):
-        out = np.zeros(4, dtype=np.uint64)
-        self._check(self._api.get_counters(self._h, _p(out, C.c_uint64), 4))
+        out = np.zeros(6, dtype=np.uint64)
+        self._check(self._api.get_counters(self._h, _p(out, C.c_uint64), 6))
         return {"logical_gates": int(out[0]), "gate_launches": int(out[1]), "gate_bytes": int(out[2]),
-                "gate_passes": int(out[3])}
+                "gate_passes": int(out[3]), "evolutions_exact": int(out[4]), "evolutions_taylor": int(out[5])}
 
     def reset_counters(self):
         self._check(self._api.reset_counters(self._h))
