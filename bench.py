@@ -357,7 +357,8 @@ def run_fused(a):
     sim = Simulator(1, precision="c64", fusion="staged")
     for q in range(nq):
         sim.allocate_qubit(q)
-    ms, cnt, recs = timed_steps(sim, gates, a.steps, a.warmup, None)
+    with ClockSampler(0) as clk:
+        ms, cnt, recs = timed_steps(sim, gates, a.steps, a.warmup, None)
     key, groups = dominant_kernel(recs)
     # the same gates without the per-group norm restoration (tensor-core mode 2)
     sim.set_tensor_cores(True, renorm=False)
@@ -394,7 +395,8 @@ def run_fused(a):
                       "without_norm_restoration": {
                           "ms_per_step": ms_nr / a.steps,
                           "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups_nr.items()}},
-                      "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()}}), flush=True)
+                      "kernel_groups": {f"kind{k[0]}_k{k[1]}_p{k[2]}": v for k, v in groups.items()},
+                      "clocks": clk.summary()}), flush=True)
 
 
 def run_gates(a):

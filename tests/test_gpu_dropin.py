@@ -93,10 +93,13 @@ def test_unitary_matches_reference_class_on_random_circuits():
         assert np.max(np.abs(ours.unitary - ref.unitary)) < 1e-12
 
 
-def test_time_evolution_against_scipy_expm():
+@pytest.mark.parametrize("hamiltonian", ["reference", "commuting"])
+def test_time_evolution_against_scipy_expm(hamiltonian):
     """The reference's time-evolution check (_simulator_test.py:514-570) with
     NumPy-2-safe array conversion: controlled exp(-i t H) on 8 qubits vs
-    scipy.sparse.linalg.expm_multiply."""
+    scipy.sparse.linalg.expm_multiply; with the reference's four-term H (the
+    Taylor series) and with a Hamiltonian whose terms commute (the exact
+    product of term exponentials)."""
     if not projectq_available():
         pytest.skip("ProjectQ not importable")
     import scipy.sparse
@@ -119,13 +122,22 @@ def test_time_evolution_against_scipy_expm():
         eng.flush()
         bitmap, init = backend.cheat()
         init = np.asarray(init).copy()
-        op = 0.3 * QubitOperator("X0 Y1 Z2 Y3 X4") + 1.1 * QubitOperator(()) \
-            - 1.4 * QubitOperator("Y0 Z1 X3 Y5") - 1.1 * QubitOperator("Y1 X2 X3 Y4")
+        if hamiltonian == "reference":
+            op = 0.3 * QubitOperator("X0 Y1 Z2 Y3 X4") + 1.1 * QubitOperator(()) \
+                - 1.4 * QubitOperator("Y0 Z1 X3 Y5") - 1.1 * QubitOperator("Y1 X2 X3 Y4")
+        else:
+            op = 0.5 * QubitOperator("Z0 Z1") - 0.7 * QubitOperator("X0 X1") + 0.4 * QubitOperator("Y0 Y1") \
+                + 1.1 * QubitOperator(()) + 0.3 * QubitOperator("Z2 Z3 Z4") + 0.2 * QubitOperator("X5 X6 X7") \
+                - 0.6 * QubitOperator("Z5 Z6")
         ctrl = eng.allocate_qubit()
         H | ctrl
+        before = backend._simulator.counters()
         with Control(eng, ctrl):
             TimeEvolution(t, op) | qureg
         eng.flush()
+        after = backend._simulator.counters()
+        path = "evolutions_taylor" if hamiltonian == "reference" else "evolutions_exact"
+        assert after[path] == before[path] + 1
         bitmap2, final = backend.cheat()
         final = np.asarray(final).copy()
         All(Measure) | qureg + ctrl
