@@ -72,7 +72,8 @@ def parse():
                          "cores; adjoint: energy + gradient of a 960-parameter ansatz at 24 qubits; learned: "
                          "learned vs greedy fusion planning on random circuits; gates: HBM bandwidth of the "
                          "single-gate kernels (one pass per gate); evolution: QAOA-style time evolution of "
-                         "commuting Hamiltonians, exact product vs Taylor series")
+                         "commuting Hamiltonians, exact product vs Taylor series, and a non-commuting one, "
+                         "Chebyshev expansion vs Taylor series")
     ap.add_argument("--ngates", type=int, default=60, help="fused workload: gates per step")
     return ap.parse_args()
 
@@ -612,6 +613,30 @@ def run_evolution(a):
     out[f"speedup_exact_vs_taylor_{n2}q"] = res["taylor"][0] / res["exact"][0]
     out[f"one_minus_fidelity_exact_vs_taylor_{n2}q"] = float(
         1 - abs(np.vdot(b_, a_)) ** 2 / (np.vdot(a_, a_).real * np.vdot(b_, b_).real))
+    # a non-commuting 50-term random Pauli Hamiltonian (the learned-planner
+    # workload's time evolution): Taylor series against the Chebyshev expansion
+    from projectq_gb300.workloads import random_pauli_hamiltonian
+
+    ham = [(tuple(t), c) for t, c in random_pauli_hamiltonian(n2, nterms=50, seed=7)]
+    res = {}
+    for mode in ("taylor", "chebyshev"):
+        sim = engine(n2, "c128")
+        sim.set_time_evolution(mode)
+        for q in range(n2):
+            sim.apply_controlled_gate(had, [q], [])
+        sim.run()
+        sim.synchronize()
+        t0 = time.perf_counter()
+        sim.emulate_time_evolution(ham, 0.5, list(range(n2)), [])
+        sim.synchronize()
+        res[mode] = (time.perf_counter() - t0, sim.cheat()[1])
+        sim.close()
+    a_, b_ = res["chebyshev"][1], res["taylor"][1]
+    out[f"noncommuting_50_terms_{n2}q"] = {
+        "t": 0.5, "sum_abs_coeffs": float(sum(abs(c) for t, c in ham if t)),
+        "taylor_seconds": res["taylor"][0], "chebyshev_seconds": res["chebyshev"][0],
+        "speedup": res["taylor"][0] / res["chebyshev"][0],
+        "max_abs_diff": float(np.max(np.abs(a_ - b_)))}
     print(json.dumps(out), flush=True)
 
 

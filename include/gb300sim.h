@@ -220,7 +220,10 @@ GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int mode);
  * pairwise and none acts on a control (the commuting case that ProjectQ's
  * setups/decompositions/time_evolution.py:28-52 decomposes), else as mode 0;
  * mode 0 always by the Taylor series of simulator.hpp:386-438 (the two agree to
- * the series' truncation, about 1e-12). */
+ * the series' truncation, about 1e-12); mode 2 as mode 1, but non-commuting
+ * terms by the Chebyshev expansion of exp(-i t H) (Bessel coefficients,
+ * truncated at 1e-16): about |t| sum|c| + 40 applications of H where the
+ * series takes about 16 |t| sum|c|. */
 GSIM_API int gsim_set_time_evolution(gsim_engine *e, int mode);
 
 /* How set_wavefunction moves a host state that is already in the engine's
@@ -240,7 +243,7 @@ GSIM_API int gsim_reserve(gsim_engine *e, uint32_t nqubits);
  *  out[2] algorithmic bytes moved by gate kernels (2 x touched amplitudes
  *  x bytes per amplitude), out[3] gate passes over the state, out[4] time
  *  evolutions applied as a product of term exponentials, out[5] time
- *  evolutions by the Taylor series. */
+ *  evolutions by the Taylor series, out[6] by the Chebyshev expansion. */
 GSIM_API int gsim_get_counters(gsim_engine *e, uint64_t *out, size_t n);
 GSIM_API int gsim_reset_counters(gsim_engine *e);
 

@@ -22,6 +22,7 @@
 #include "../../include/gb300sim.h"
 #include "fusion.hpp"
 #include "kernels.hpp"
+#include "pauli.hpp"
 #include "stage.hpp"
 
 namespace gsim {
@@ -86,12 +87,6 @@ struct HostBuf {
     p = nullptr;
     bytes = 0;
   }
-};
-
-struct PauliTerm {
-  uint64_t xmask = 0, sign_mask = 0;
-  int ny = 0;          // phase (-i)^ny
-  bool empty = false;  // no factors: the identity term of simulator.hpp:394-395
 };
 
 class Engine {
@@ -435,11 +430,8 @@ class Engine {
     }
     if (ks.empty()) return false;
     for (size_t a = 0; a < ks.size(); ++a)
-      for (size_t b = a + 1; b < ks.size(); ++b) {
-        const PauliTerm &p = terms[ks[a]], &q = terms[ks[b]];
-        if ((__builtin_popcountll(p.xmask & q.sign_mask) + __builtin_popcountll(p.sign_mask & q.xmask)) & 1)
-          return false;
-      }
+      for (size_t b = a + 1; b < ks.size(); ++b)
+        if (!paulis_commute(terms[ks[a]], terms[ks[b]])) return false;
     std::vector<unsigned> id_at(N_, 0);
     for (auto const &kv : map_) id_at[kv.second] = kv.first;
     static const cplx ph[4] = {cplx(1, 0), cplx(0, -1), cplx(-1, 0), cplx(0, 1)};  // (-i)^ny
@@ -452,8 +444,7 @@ class Engine {
       const uint64_t supp = p.xmask | p.sign_mask;
       const unsigned w = unsigned(__builtin_popcountll(supp));
       if (w <= kTermGateQubits) {
-        // the gate on the support, local bit i = i-th lowest support position:
-        // M = a I + b X^x Z^z with (X^x Z^z)[r][r ^ x] = (-1)^{popcount(r & z)}
+        // the gate on the support, local bit i = i-th lowest support position
         std::vector<unsigned> ids, at;
         for (unsigned q = 0; q < N_; ++q)
           if ((supp >> q) & 1) {
@@ -465,13 +456,7 @@ class Engine {
           lx |= uint32_t((p.xmask >> at[i]) & 1) << i;
           lz |= uint32_t((p.sign_mask >> at[i]) & 1) << i;
         }
-        const size_t d = size_t(1) << w;
-        std::vector<cplx> m(d * d, cplx(0., 0.));
-        for (size_t r = 0; r < d; ++r) {
-          m[r * d + r] += a;
-          m[r * d + (r ^ lx)] += (__builtin_popcount(uint32_t(r) & lz) & 1) ? -b : b;
-        }
-        submit_gate(std::move(m), ids, ctrl);
+        submit_gate(pauli_exp_matrix(w, lx, lz, a, b), ids, ctrl);
       } else {
         run();
         PauliRotationDev rd{};
@@ -504,21 +489,21 @@ class Engine {
     run();
     uint64_t cm = 0;
     for (unsigned c : ctrl) cm |= uint64_t(1) << pos_of(c);
-    if (te_mode_ == 1 && evolve_commuting(terms, coeffs, time, ctrl, cm)) return;
-    counters_[5] += 1;
+    if (te_mode_ >= 1 && evolve_commuting(terms, coeffs, time, ctrl, cm)) return;
+    counters_[te_mode_ == 2 ? 6 : 5] += 1;
     double tr = 0., op_nrm = 0.;
-    std::vector<PauliApplyTermDev> dev;
+    std::vector<PauliRealTermDev> dev;
     for (size_t t = 0; t < terms.size(); ++t) {
       if (terms[t].empty) {
         tr += coeffs[t];
       } else {
-        dev.push_back(apply_term_dev(terms[t], cplx(coeffs[t], 0.)));
+        dev.push_back(PauliRealTermDev{terms[t].xmask, terms[t].sign_mask, coeffs[t], terms[t].ny & 3, 0});
         op_nrm += std::abs(coeffs[t]);
       }
     }
-    // group terms that share a flip mask (one gather per group in the kernel)
+    // terms that share a flip mask next to each other (their gathers hit L1)
     std::stable_sort(dev.begin(), dev.end(),
-                     [](const PauliApplyTermDev &a, const PauliApplyTermDev &b) { return a.xmask < b.xmask; });
+                     [](const PauliRealTermDev &a, const PauliRealTermDev &b) { return a.xmask < b.xmask; });
     const unsigned s = unsigned(std::abs(time) * op_nrm + 1.);
     const cplx I(0., 1.);
     const cplx corr = std::exp(-time * I * tr / double(s));
@@ -527,16 +512,34 @@ class Engine {
     auto *nxt = static_cast<double2 *>(aux2_.get(n * 16));
     auto *out = static_cast<double2 *>(scratch_c128(n));
     CK(launch_convert(0, vec, prec_ == GSIM_C64 ? 1 : 0, state_.p, n, stream_));
-    CK(cudaMemcpyAsync(out, vec, n * 16, cudaMemcpyDeviceToDevice, stream_));
-    auto *d_terms = static_cast<PauliApplyTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliApplyTermDev)));
+    auto *d_terms = static_cast<PauliRealTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliRealTermDev)));
     if (!dev.empty())
       CK(cudaMemcpyAsync(d_terms, dev.data(), dev.size() * sizeof(dev[0]), cudaMemcpyHostToDevice, stream_));
+    if (te_mode_ == 2) {
+      evolve_chebyshev(vec, nxt, out, d_terms, int(dev.size()), op_nrm, time, tr, cm);
+    } else {
+      CK(cudaMemcpyAsync(out, vec, n * 16, cudaMemcpyDeviceToDevice, stream_));
+      taylor_steps(vec, nxt, out, d_terms, int(dev.size()), s, time, corr, cm);
+    }
+    CK(launch_convert(prec_ == GSIM_C64 ? 1 : 0, state_.p, 0, out, n, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    // aux1_/aux2_ hold two full complex128 vectors: give the memory back.
+    aux1_.release();
+    aux2_.release();
+  }
+
+  // The reference's series: s steps, each summed until the controlled part of
+  // an order's update has norm <= 1e-12, then the identity terms' phase.
+  void taylor_steps(double2 *vec, double2 *nxt, double2 *out, const PauliRealTermDev *d_terms, int nterms,
+                    unsigned s, double time, cplx corr, uint64_t cm) {
+    const cplx I(0., 1.);
+    const size_t n = size_t(1) << N_;
     double *d_norm = static_cast<double *>(small_.get(4096));
     for (unsigned i = 0; i < s; ++i) {
       double nrm_change = 1.;
       for (unsigned k = 0; nrm_change > 1.e-12; ++k) {
         const cplx coeff = (-time * I) / double(s * (k + 1));
-        CK(launch_taylor_step(vec, nxt, out, N_, d_terms, int(dev.size()), coeff.real(), coeff.imag(),
+        CK(launch_taylor_step(vec, nxt, out, N_, d_terms, nterms, coeff.real(), coeff.imag(),
                               cm, part(), d_norm, stream_));
         std::swap(vec, nxt);
         double h = 0.;
@@ -547,11 +550,34 @@ class Engine {
       }
       CK(launch_phase_ctrl(out, vec, n, cm, corr.real(), corr.imag(), stream_));
     }
-    CK(launch_convert(prec_ == GSIM_C64 ? 1 : 0, state_.p, 0, out, n, stream_));
-    CK(cudaStreamSynchronize(stream_));
-    // aux1_/aux2_ hold two full complex128 vectors: give the memory back.
-    aux1_.release();
-    aux2_.release();
+  }
+
+  // exp(-i t H') psi by its Chebyshev expansion (Jacobi-Anger):
+  //   exp(-i tau x) = J_0(tau) + 2 sum_{k>=1} (-i)^k J_k(tau) T_k(x),
+  // with A = H' / beta (beta = sum |c_t| >= ||H'||, so ||A|| <= 1), tau =
+  // t beta, T_k(A) psi by u_{k+1} = 2 A u_k - u_{k-1}, truncated where the
+  // remaining coefficients sum below 1e-16 (each ||T_k(A) psi|| <= 1).  About
+  // |tau| + 40 applications of H' where the series needs ~16 |tau|.  Then the
+  // identity terms' phase exp(-i t tr) on the controlled part.
+  void evolve_chebyshev(double2 *vec, double2 *nxt, double2 *out, const PauliRealTermDev *d_terms, int nterms,
+                        double beta, double time, double tr, uint64_t cm) {
+    const size_t n = size_t(1) << N_;
+    const double tau = time * beta;
+    std::vector<double> J = bessel_j_orders(std::abs(tau), 1e-16);
+    if (tau < 0)
+      for (size_t k = 1; k < J.size(); k += 2) J[k] = -J[k];
+    static const cplx mi[4] = {cplx(1, 0), cplx(0, -1), cplx(-1, 0), cplx(0, 1)};  // (-i)^k
+    CK(launch_scale_ctrl(vec, out, n, cm, J[0], 0., stream_));
+    double2 *cur = vec, *other = nxt;
+    for (size_t k = 1; k < J.size(); ++k) {
+      const cplx a = 2. * J[k] * mi[k & 3];
+      // k = 1: other <- A u_0; k >= 2: other (holding u_{k-2}) <- 2 A u_{k-1} - u_{k-2}
+      CK(launch_chebyshev_step(cur, other, out, N_, d_terms, nterms, (k == 1 ? 1. : 2.) / beta, k >= 2,
+                               a.real(), a.imag(), cm, stream_));
+      std::swap(cur, other);
+    }
+    const cplx corr = std::exp(cplx(0., -time * tr));
+    CK(launch_phase_ctrl(out, vec, n, cm, corr.real(), corr.imag(), stream_));
   }
 
   // ---- simulator.hpp:352-368 ----------------------------------------------
@@ -798,7 +824,9 @@ class Engine {
   }
 
   void set_time_evolution(int mode) {
-    if (mode != 0 && mode != 1) fail(GSIM_ERR_VALUE, "time-evolution mode must be 0 (Taylor series) or 1 (exact for commuting terms)");
+    if (mode < 0 || mode > 2)
+      fail(GSIM_ERR_VALUE, "time-evolution mode must be 0 (Taylor series), 1 (exact for commuting terms, else "
+                           "Taylor) or 2 (exact for commuting terms, else Chebyshev)");
     te_mode_ = mode;
   }
 
@@ -836,7 +864,7 @@ class Engine {
     prof_.clear();
     ev_next_ = 0;
   }
-  uint64_t counter(size_t i) const { return i < 6 ? counters_[i] : 0; }
+  uint64_t counter(size_t i) const { return i < 7 ? counters_[i] : 0; }
   void reset_counters() { std::fill(std::begin(counters_), std::end(counters_), 0); }
 
  private:
@@ -1145,7 +1173,7 @@ class Engine {
   bool use_reg_stages_ = true;
   bool use_tc_ = true;
   int tc_mode_ = 1;
-  int te_mode_ = 1;  // emulate_time_evolution: 0 Taylor series only, 1 exact product for commuting terms
+  int te_mode_ = 1;  // emulate_time_evolution: 0 Taylor only, 1 exact for commuting terms else Taylor, 2 ... else Chebyshev
   int upload_mode_ = 1;  // host -> device state copies: 0 copy engine, 1 SM reads of page-locked memory
   bool tc_used_ = false;
   std::array<UploadSlot, 4> mslots_;
@@ -1159,7 +1187,7 @@ class Engine {
   DevBuf upload_dev_;
   HostBuf upload_host_;
   cudaEvent_t upload_ev_ = nullptr;
-  uint64_t counters_[6] = {0, 0, 0, 0, 0, 0};
+  uint64_t counters_[7] = {0, 0, 0, 0, 0, 0, 0};
   // timing
   cudaEvent_t timer_[16] = {};
   struct Prof {
@@ -1752,39 +1780,24 @@ std::vector<unsigned> vu(const uint32_t *p, size_t n) {
 }
 std::vector<unsigned> reg_sizes(const uint32_t *s, size_t n) { return vu(s, n); }
 
-// Pauli terms in CSR form -> engine terms (positions resolved through ids).
-// A term's factors are applied in order, as apply_term does through the gate
-// path (simulator.hpp:538-550), so the product is F_last ... F_first.  It is
-// kept as i^k X^x Z^z (per qubit X^{x_q} Z^{z_q}); Y = i X Z, and moving a new
-// factor's Z past an existing X costs a sign.  Then
-//   (X^x Z^z psi)_i = (-1)^{popcount(x & z)} (-1)^{popcount(i & z)} psi_{i ^ x},
-// and the kernels use P psi = (-i)^{ny} (-1)^{popcount(i & z)} psi_{i ^ x}.
+// Pauli terms in CSR form -> engine terms (positions resolved through ids,
+// factors combined by pauli_term_of in the order given).
 std::vector<gsim::PauliTerm> terms_of(Engine *eng, const uint32_t *off, const uint32_t *q,
                                       const uint8_t *pa, size_t nterms, const uint32_t *ids,
                                       size_t nids) {
   const std::map<unsigned, unsigned> &m = eng->mapping();
   std::vector<gsim::PauliTerm> out(nterms);
+  std::vector<std::pair<unsigned, char>> factors;
   for (size_t t = 0; t < nterms; ++t) {
-    gsim::PauliTerm pt;
-    pt.empty = off[t + 1] == off[t];
-    int k = 0;
+    factors.clear();
     for (uint32_t f = off[t]; f < off[t + 1]; ++f) {
       if (q[f] >= nids) gsim::fail(GSIM_ERR_VALUE, "Pauli term acts on a qubit index outside the qureg");
       auto it = m.find(ids[q[f]]);
       if (it == m.end())
         gsim::fail(GSIM_ERR_RUNTIME, "Unknown qubit id. Please make sure you have called eng.flush().");
-      const uint64_t bit = uint64_t(1) << it->second;
-      const char c = char(pa[f]);
-      if (c != 'X' && c != 'Y' && c != 'Z') gsim::fail(GSIM_ERR_VALUE, "Pauli must be X, Y or Z");
-      const bool fx = c == 'X' || c == 'Y', fz = c == 'Z' || c == 'Y';
-      if (c == 'Y') k += 1;
-      if (fz && (pt.xmask & bit)) k += 2;
-      if (fx) pt.xmask ^= bit;
-      if (fz) pt.sign_mask ^= bit;
+      factors.emplace_back(it->second, char(pa[f]));
     }
-    const int ipow = (k + 2 * (__builtin_popcountll(pt.xmask & pt.sign_mask) & 1)) & 3;
-    pt.ny = (4 - ipow) & 3;  // (-i)^ny == i^ipow
-    out[t] = pt;
+    if (!gsim::pauli_term_of(factors, out[t])) gsim::fail(GSIM_ERR_VALUE, "Pauli must be X, Y or Z");
   }
   return out;
 }

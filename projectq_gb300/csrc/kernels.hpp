@@ -99,16 +99,37 @@ struct PauliApplyTermDev {
 cudaError_t launch_pauli_apply(int prec, const void *in, void *out, unsigned nq,
                                const PauliApplyTermDev *d_terms, int nterms, cudaStream_t s);
 
+// A term with a real coefficient r (a Hamiltonian's): r P with
+// P = (-i)^ny X^x Z^sign_mask.  (-i)^ny only swaps and negates the real and
+// imaginary parts, so the kernels spend 2 FP64 FMAs per term and amplitude.
+struct PauliRealTermDev {
+  uint64_t xmask;
+  uint64_t sign_mask;
+  double r;
+  int32_t ny;
+  int32_t pad;
+};
+
 // One Taylor order of emulate_time_evolution, all FP64 (complex128 vectors):
 //   upd_j = coeff * sum_t c_t (P_t vec)_j ; vec_next_j = upd_j ;
 //   where (j & ctrl) == ctrl: out_j += upd_j and part += |upd_j|^2.
 cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *out, unsigned nq,
-                               const PauliApplyTermDev *d_terms, int nterms, double coeff_re,
+                               const PauliRealTermDev *d_terms, int nterms, double coeff_re,
                                double coeff_im, uint64_t ctrl, double *d_part, double *d_norm,
                                cudaStream_t s);
 // out_j *= corr where (j & ctrl) == ctrl; vec_j = out_j.
 cudaError_t launch_phase_ctrl(double2 *out, double2 *vec, uint64_t n, uint64_t ctrl, double cre,
                               double cim, cudaStream_t s);
+
+// One order of the Chebyshev expansion of exp(-i t H) (complex128 vectors):
+//   w_j = scale * sum_t c_t (P_t cur)_j - prev_j   (no prev term if !has_prev),
+//   prev_j <- w_j, and where (j & ctrl) == ctrl: out_j += a w_j.
+cudaError_t launch_chebyshev_step(const double2 *cur, double2 *prev, double2 *out, unsigned nq,
+                                  const PauliRealTermDev *d_terms, int nterms, double scale, bool has_prev,
+                                  double a_re, double a_im, uint64_t ctrl, cudaStream_t s);
+// out_j = a psi_j where (j & ctrl) == ctrl, psi_j elsewhere.
+cudaError_t launch_scale_ctrl(const double2 *psi, double2 *out, uint64_t n, uint64_t ctrl, double a_re,
+                              double a_im, cudaStream_t s);
 
 // One Pauli exponential in place, on the amplitudes whose control bits are
 // all set:  psi <- a psi + b P psi, with (P psi)_j = (-1)^{popcount(j & z)}

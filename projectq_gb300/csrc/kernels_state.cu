@@ -350,57 +350,112 @@ __global__ void __launch_bounds__(256) pauli_expect_kernel(const cplx_t<T> *__re
   }
 }
 
+// ---- sums of Pauli strings ------------------------------------------------
+// Up to kSmemTerms terms are staged in shared memory per block (the rest of a
+// longer list is read through L1).  Each thread issues the gathers of four
+// terms before it uses them, so four loads per thread are in flight; terms
+// sharing a flip mask gather the same address (an L1 hit).  The terms are
+// summed in list order.
+constexpr int kSmemTerms = 1024;
+
+// Dynamic shared memory of a launch: term_smem_bytes<Term>(nterms).
+template <typename Term>
+__device__ __forceinline__ const Term *stage_terms(const Term *__restrict__ terms, int nterms) {
+  if (nterms > kSmemTerms) return terms;
+  extern __shared__ __align__(16) unsigned char term_smem[];
+  auto *sm = reinterpret_cast<Term *>(term_smem);
+  for (int t = threadIdx.x; t < nterms; t += blockDim.x) sm[t] = terms[t];
+  __syncthreads();
+  return sm;
+}
+template <typename Term> size_t term_smem_bytes(int nterms) {
+  return nterms > kSmemTerms ? 0 : size_t(nterms) * sizeof(Term);
+}
+
+// sum_t r_t (P_t v)_j in FP64 for real-coefficient terms: with a = v.x, b =
+// v.y (ny even) or a = v.y, b = v.x (ny odd), the term adds +-r a to the real
+// part and +-r b to the imaginary part; the signs ((-1)^popcount(j & z) and
+// those of (-i)^ny) are applied to r by flipping its sign bit.
+__device__ __forceinline__ double flip(double r, uint32_t neg) {
+  return __longlong_as_double(__double_as_longlong(r) ^ (static_cast<long long>(neg & 1u) << 63));
+}
+__device__ __forceinline__ void real_term_add(const PauliRealTermDev &pt, double2 g, uint64_t j, double &re,
+                                              double &im) {
+  const uint32_t par = uint32_t(__popcll(j & pt.sign_mask)) & 1u;
+  const uint32_t ny = uint32_t(pt.ny);
+  const bool odd = ny & 1u;
+  const double a = odd ? g.y : g.x, b = odd ? g.x : g.y;
+  re = fma(flip(pt.r, par ^ (ny >> 1)), a, re);               // negative for ny = 2, 3
+  im = fma(flip(pt.r, par ^ ((ny ^ (ny >> 1)) & 1u)), b, im);  // negative for ny = 1, 2
+}
+__device__ __forceinline__ void pauli_real_sum(const double2 *__restrict__ v, uint64_t j,
+                                               const PauliRealTermDev *tp, int nterms, double &re, double &im) {
+  int t = 0;
+  for (; t + 4 <= nterms; t += 4) {
+    double2 g[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) g[u] = v[j ^ tp[t + u].xmask];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) real_term_add(tp[t + u], g[u], j, re, im);
+  }
+  for (; t < nterms; ++t) real_term_add(tp[t], v[j ^ tp[t].xmask], j, re, im);
+}
+
+// sum_t c_t (P_t v)_j with (P_t v)_j = (-1)^{popcount(j & sign)} v_{j ^ x}
+// and c_t = cre + i cim (the term's phase folded in), accumulated in A.
+template <typename A, typename V>
+__device__ __forceinline__ void pauli_sum(const V *__restrict__ v, uint64_t j, const PauliApplyTermDev *tp,
+                                          int nterms, A &re, A &im) {
+  int t = 0;
+  for (; t + 4 <= nterms; t += 4) {
+    V g[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) g[u] = v[j ^ tp[t + u].xmask];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const PauliApplyTermDev &pt = tp[t + u];
+      const A sg = (__popcll(j & pt.sign_mask) & 1) ? A(-1) : A(1);
+      const A cr = A(pt.cre) * sg, ci = A(pt.cim) * sg;
+      re += cr * A(g[u].x) - ci * A(g[u].y);
+      im += cr * A(g[u].y) + ci * A(g[u].x);
+    }
+  }
+  for (; t < nterms; ++t) {
+    const PauliApplyTermDev &pt = tp[t];
+    const V g = v[j ^ pt.xmask];
+    const A sg = (__popcll(j & pt.sign_mask) & 1) ? A(-1) : A(1);
+    const A cr = A(pt.cre) * sg, ci = A(pt.cim) * sg;
+    re += cr * A(g.x) - ci * A(g.y);
+    im += cr * A(g.y) + ci * A(g.x);
+  }
+}
+
 // ---- Pauli application (apply_qubit_operator) ----------------------------
 template <typename T>
 __global__ void __launch_bounds__(256) pauli_apply_kernel(const cplx_t<T> *__restrict__ in,
                                                           cplx_t<T> *__restrict__ out, uint64_t n,
                                                           const PauliApplyTermDev *__restrict__ terms,
                                                           int nterms) {
+  const PauliApplyTermDev *tp = stage_terms<PauliApplyTermDev>(terms, nterms);
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t i = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
     T re = T(0), im = T(0);
-    for (int t = 0; t < nterms; ++t) {
-      const PauliApplyTermDev pt = terms[t];
-      const cplx_t<T> v = in[i ^ pt.xmask];
-      const T sg = (__popcll(i & pt.sign_mask) & 1) ? T(-1) : T(1);
-      const T cr = T(pt.cre) * sg, ci = T(pt.cim) * sg;
-      re += cr * v.x - ci * v.y;
-      im += cr * v.y + ci * v.x;
-    }
+    pauli_sum<T>(in, i, tp, nterms, re, im);
     out[i] = mkc<T>(re, im);
   }
 }
 
 __global__ void __launch_bounds__(256) taylor_step_kernel(
     const double2 *__restrict__ vec, double2 *__restrict__ vnext, double2 *__restrict__ out,
-    uint64_t n, const PauliApplyTermDev *__restrict__ terms, int nterms, double cre, double cim,
+    uint64_t n, const PauliRealTermDev *__restrict__ terms, int nterms, double cre, double cim,
     uint64_t ctrl, double *part) {
+  const PauliRealTermDev *tp = stage_terms<PauliRealTermDev>(terms, nterms);
   double nrm = 0.;
   const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
   for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+    // (P_t vec)_j = phase * sign * vec[j ^ x], exact; times the real c_t
     double ur = 0., ui = 0.;
-    // terms arrive grouped by flip mask: one gather per group
-    uint64_t xprev = ~uint64_t(0);
-    double2 v = make_double2(0., 0.);
-    for (int t = 0; t < nterms; ++t) {
-      const PauliApplyTermDev pt = terms[t];
-      if (pt.xmask != xprev) {
-        v = vec[j ^ pt.xmask];
-        xprev = pt.xmask;
-      }
-      const bool neg = __popcll(j & pt.sign_mask) & 1;
-      // (P_t vec)_j = phase * sign * vec[j ^ x], exact; times the real c_t.
-      // pt.cre/pt.cim hold (-i)^{#Y} and pt.sign_mask the Y|Z positions;
-      // the real coefficient is folded in by the host as a scale of both.
-      double pr = pt.cre * v.x - pt.cim * v.y;
-      double pi = pt.cre * v.y + pt.cim * v.x;
-      if (neg) {
-        pr = -pr;
-        pi = -pi;
-      }
-      ur += pr;
-      ui += pi;
-    }
+    pauli_real_sum(vec, j, tp, nterms, ur, ui);
     const double zr = ur * cre - ui * cim;
     const double zi = ur * cim + ui * cre;
     vnext[j] = make_double2(zr, zi);
@@ -414,6 +469,45 @@ __global__ void __launch_bounds__(256) taylor_step_kernel(
   }
   const double s = block_sum(nrm);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// One Chebyshev order: w = scale * sum_t c_t (P_t cur)_j - prev_j (prev not
+// read on the first order, has_prev = 0); w replaces prev in place (every
+// thread reads prev only at its own j, and gathers only from cur); where
+// (j & ctrl) == ctrl: out_j += a * w.
+__global__ void __launch_bounds__(256) chebyshev_step_kernel(
+    const double2 *__restrict__ cur, double2 *__restrict__ prev, double2 *__restrict__ out, uint64_t n,
+    const PauliRealTermDev *__restrict__ terms, int nterms, double scale, int has_prev, double are,
+    double aim, uint64_t ctrl) {
+  const PauliRealTermDev *tp = stage_terms<PauliRealTermDev>(terms, nterms);
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+    double ur = 0., ui = 0.;
+    pauli_real_sum(cur, j, tp, nterms, ur, ui);
+    double wr = scale * ur, wi = scale * ui;
+    if (has_prev) {
+      const double2 p = prev[j];
+      wr -= p.x;
+      wi -= p.y;
+    }
+    prev[j] = make_double2(wr, wi);
+    if ((j & ctrl) == ctrl) {
+      double2 o = out[j];
+      o.x += are * wr - aim * wi;
+      o.y += are * wi + aim * wr;
+      out[j] = o;
+    }
+  }
+}
+
+// out_j = a * psi_j where (j & ctrl) == ctrl, else psi_j.
+__global__ void scale_ctrl_kernel(const double2 *__restrict__ psi, double2 *__restrict__ out, uint64_t n,
+                                  uint64_t ctrl, double are, double aim) {
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t j = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; j < n; j += stride) {
+    const double2 p = psi[j];
+    out[j] = (j & ctrl) == ctrl ? make_double2(are * p.x - aim * p.y, are * p.y + aim * p.x) : p;
+  }
 }
 
 // psi <- a psi + b P psi over the controlled subspace.  With x != 0 a thread
@@ -716,19 +810,19 @@ cudaError_t launch_pauli_apply(int prec, const void *in, void *out, unsigned nq,
                                const PauliApplyTermDev *d_terms, int nterms, cudaStream_t s) {
   const uint64_t n = uint64_t(1) << nq;
   if (prec == 1)
-    pauli_apply_kernel<float><<<grid(n, 256), 256, 0, s>>>(static_cast<const float2 *>(in), static_cast<float2 *>(out), n, d_terms, nterms);
+    pauli_apply_kernel<float><<<grid(n, 256), 256, term_smem_bytes<PauliApplyTermDev>(nterms), s>>>(static_cast<const float2 *>(in), static_cast<float2 *>(out), n, d_terms, nterms);
   else
-    pauli_apply_kernel<double><<<grid(n, 256), 256, 0, s>>>(static_cast<const double2 *>(in), static_cast<double2 *>(out), n, d_terms, nterms);
+    pauli_apply_kernel<double><<<grid(n, 256), 256, term_smem_bytes<PauliApplyTermDev>(nterms), s>>>(static_cast<const double2 *>(in), static_cast<double2 *>(out), n, d_terms, nterms);
   return cudaGetLastError();
 }
 
 cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *out, unsigned nq,
-                               const PauliApplyTermDev *d_terms, int nterms, double coeff_re,
+                               const PauliRealTermDev *d_terms, int nterms, double coeff_re,
                                double coeff_im, uint64_t ctrl, double *d_part, double *d_norm,
                                cudaStream_t s) {
   const uint64_t n = uint64_t(1) << nq;
   const unsigned g = std::min<unsigned>(grid(n, 256), kPartMax);
-  taylor_step_kernel<<<g, 256, 0, s>>>(vec, vec_next, out, n, d_terms, nterms, coeff_re, coeff_im, ctrl, d_part);
+  taylor_step_kernel<<<g, 256, term_smem_bytes<PauliRealTermDev>(nterms), s>>>(vec, vec_next, out, n, d_terms, nterms, coeff_re, coeff_im, ctrl, d_part);
   column_sums_kernel<<<1, 1024, 0, s>>>(d_part, int(g), d_norm);
   return cudaGetLastError();
 }
@@ -736,6 +830,21 @@ cudaError_t launch_taylor_step(const double2 *vec, double2 *vec_next, double2 *o
 cudaError_t launch_phase_ctrl(double2 *out, double2 *vec, uint64_t n, uint64_t ctrl, double cre,
                               double cim, cudaStream_t s) {
   phase_ctrl_kernel<<<grid(n, 256), 256, 0, s>>>(out, vec, n, ctrl, cre, cim);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_chebyshev_step(const double2 *cur, double2 *prev, double2 *out, unsigned nq,
+                                  const PauliRealTermDev *d_terms, int nterms, double scale, bool has_prev,
+                                  double a_re, double a_im, uint64_t ctrl, cudaStream_t s) {
+  const uint64_t n = uint64_t(1) << nq;
+  chebyshev_step_kernel<<<grid(n, 256), 256, term_smem_bytes<PauliRealTermDev>(nterms), s>>>(cur, prev, out, n, d_terms, nterms, scale, has_prev ? 1 : 0,
+                                                     a_re, a_im, ctrl);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scale_ctrl(const double2 *psi, double2 *out, uint64_t n, uint64_t ctrl, double a_re,
+                              double a_im, cudaStream_t s) {
+  scale_ctrl_kernel<<<grid(n, 256), 256, 0, s>>>(psi, out, n, ctrl, a_re, a_im);
   return cudaGetLastError();
 }
 

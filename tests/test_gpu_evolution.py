@@ -229,3 +229,50 @@ def test_qaoa_layers_share_stage_passes():
     a, b = g.cheat()[1].astype(np.complex128), r.cheat()[1]
     fid = abs(np.vdot(b, a)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real)
     assert 1 - fid < 1e-6, 1 - fid
+
+
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+@pytest.mark.parametrize("t", [1.3, -0.7, 6.0])
+def test_chebyshev_expansion_for_anticommuting_terms(prec, t):
+    """Mode "chebyshev": non-commuting terms by the Chebyshev expansion, against
+    scipy's expm (1e-12) and the oracle's series (1e-11); controlled; up to
+    |t| sum|c| of about 40."""
+    n = 8
+    terms = random_pauli_sum(n - 1, 8, seed=21)
+    gates = random_mixed_circuit(n, 30, 5, kmax=2, max_ctrl=1)
+    g = make("gpu", seed=1, precision=prec)
+    o = make("oracle", seed=1)
+    g.set_time_evolution("chebyshev")
+    for s in (g, o):
+        allocate(s, n)
+        run_circuit(s, gates)
+    _, before = g.cheat()
+    for s in (g, o):
+        s.emulate_time_evolution(terms, t, list(range(n - 1)), [n - 1])
+    c = g.counters()
+    assert c["evolutions_chebyshev"] == 1 and c["evolutions_taylor"] == 0
+    err = float(np.max(np.abs(g.cheat()[1] - o.cheat()[1])))
+    assert err <= TOL_ORACLE[prec], err
+    if prec == "c128":
+        want = expected(before, terms, t, n - 1, ctrl_bit=n - 1)
+        err = float(np.max(np.abs(g.cheat()[1] - want)))
+        assert err <= 1e-12, err
+
+
+def test_chebyshev_mode_identity_and_commuting():
+    """Identity-only Hamiltonians (a phase) and commuting ones (the exact
+    product) behave in mode "chebyshev" as in the default mode."""
+    n = 6
+    gates = random_mixed_circuit(n, 20, 6, kmax=2, max_ctrl=1)
+    rng = np.random.default_rng(3)
+    for tm, path in (([([], 0.9), ([], -0.2)], "evolutions_chebyshev"), (ising(n - 1, rng), "evolutions_exact")):
+        g = make("gpu", seed=1, precision="c128")
+        o = make("oracle", seed=1)
+        g.set_time_evolution("chebyshev")
+        for s in (g, o):
+            allocate(s, n)
+            run_circuit(s, gates)
+            s.emulate_time_evolution(tm, 0.8, list(range(n - 1)), [n - 1])
+        assert g.counters()[path] == 1
+        err = float(np.max(np.abs(g.cheat()[1] - o.cheat()[1])))
+        assert err <= 1e-11, err
