@@ -55,6 +55,15 @@ template <> struct NormAcc<float> {
   __device__ double get() const { return s + double(f); }
 };
 
+// x with its sign bit flipped when neg & 1 (integer work, no floating-point
+// multiply).
+__device__ __forceinline__ double flip(double r, uint32_t neg) {
+  return __longlong_as_double(__double_as_longlong(r) ^ (static_cast<long long>(neg & 1u) << 63));
+}
+__device__ __forceinline__ float flip(float r, uint32_t neg) {
+  return __int_as_float(__float_as_int(r) ^ static_cast<int>((neg & 1u) << 31));
+}
+
 struct MaskSpec {
   uint8_t pos[64];
   int n;
@@ -331,8 +340,8 @@ __global__ void __launch_bounds__(256) pauli_expect_kernel(const cplx_t<T> *__re
     for (int t = 0; t < kTermsPerLaunch; ++t) {
       if (t < B.nterms) {
         const T v = B.t[t].which ? ai : ar;
-        const T sg = (__popcll(i & B.t[t].sign_mask) & 1) ? T(-1) : T(1);
-        mini[t] = fma(sg * T(B.t[t].factor), v, mini[t]);
+        const uint32_t neg = uint32_t(__popcll(i & B.t[t].sign_mask)) & 1u;
+        mini[t] = fma(flip(T(B.t[t].factor), neg), v, mini[t]);
       }
     }
     if (++cnt == 8) {
@@ -376,9 +385,6 @@ template <typename Term> size_t term_smem_bytes(int nterms) {
 // v.y (ny even) or a = v.y, b = v.x (ny odd), the term adds +-r a to the real
 // part and +-r b to the imaginary part; the signs ((-1)^popcount(j & z) and
 // those of (-i)^ny) are applied to r by flipping its sign bit.
-__device__ __forceinline__ double flip(double r, uint32_t neg) {
-  return __longlong_as_double(__double_as_longlong(r) ^ (static_cast<long long>(neg & 1u) << 63));
-}
 __device__ __forceinline__ void real_term_add(const PauliRealTermDev &pt, double2 g, uint64_t j, double &re,
                                               double &im) {
   const uint32_t par = uint32_t(__popcll(j & pt.sign_mask)) & 1u;
@@ -401,8 +407,15 @@ __device__ __forceinline__ void pauli_real_sum(const double2 *__restrict__ v, ui
   for (; t < nterms; ++t) real_term_add(tp[t], v[j ^ tp[t].xmask], j, re, im);
 }
 
-// sum_t c_t (P_t v)_j with (P_t v)_j = (-1)^{popcount(j & sign)} v_{j ^ x}
-// and c_t = cre + i cim (the term's phase folded in), accumulated in A.
+// c_t (P_t v)_j with (P_t v)_j = (-1)^{popcount(j & sign)} v_{j ^ x} and
+// c_t = cre + i cim (the term's phase folded in), accumulated in A: 4 FMAs.
+template <typename A, typename V>
+__device__ __forceinline__ void complex_term_add(const PauliApplyTermDev &pt, V g, uint64_t j, A &re, A &im) {
+  const uint32_t par = uint32_t(__popcll(j & pt.sign_mask)) & 1u;
+  const A cr = flip(A(pt.cre), par), ci = flip(A(pt.cim), par);
+  re = fma(cr, A(g.x), fma(-ci, A(g.y), re));
+  im = fma(cr, A(g.y), fma(ci, A(g.x), im));
+}
 template <typename A, typename V>
 __device__ __forceinline__ void pauli_sum(const V *__restrict__ v, uint64_t j, const PauliApplyTermDev *tp,
                                           int nterms, A &re, A &im) {
@@ -412,22 +425,9 @@ __device__ __forceinline__ void pauli_sum(const V *__restrict__ v, uint64_t j, c
 #pragma unroll
     for (int u = 0; u < 4; ++u) g[u] = v[j ^ tp[t + u].xmask];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const PauliApplyTermDev &pt = tp[t + u];
-      const A sg = (__popcll(j & pt.sign_mask) & 1) ? A(-1) : A(1);
-      const A cr = A(pt.cre) * sg, ci = A(pt.cim) * sg;
-      re += cr * A(g[u].x) - ci * A(g[u].y);
-      im += cr * A(g[u].y) + ci * A(g[u].x);
-    }
+    for (int u = 0; u < 4; ++u) complex_term_add(tp[t + u], g[u], j, re, im);
   }
-  for (; t < nterms; ++t) {
-    const PauliApplyTermDev &pt = tp[t];
-    const V g = v[j ^ pt.xmask];
-    const A sg = (__popcll(j & pt.sign_mask) & 1) ? A(-1) : A(1);
-    const A cr = A(pt.cre) * sg, ci = A(pt.cim) * sg;
-    re += cr * A(g.x) - ci * A(g.y);
-    im += cr * A(g.y) + ci * A(g.x);
-  }
+  for (; t < nterms; ++t) complex_term_add(tp[t], v[j ^ tp[t].xmask], j, re, im);
 }
 
 // ---- Pauli application (apply_qubit_operator) ----------------------------
