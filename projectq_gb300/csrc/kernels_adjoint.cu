@@ -32,15 +32,42 @@ struct AdjStep {
   int col;           // output column of the partial sums
 };
 
-template <typename T>
+// (a, b) <- U^dagger (a, b) by matrix class (chosen on the host from exact
+// zeros and ones of U^dagger; each class drops only terms that are exactly
+// zero, so all classes give the general formula's values):
+// 0 general, 1 real (Ry), 2 real diagonal / imaginary off-diagonal (Rx),
+// 3 diagonal (Rz, Ph, R), 4 exact swap (X, CNOT).
+template <typename T, int CLS>
 __device__ __forceinline__ void mv(const AdjStep &S, cplx_t<T> &a, cplx_t<T> &b) {
   const T u00r = T(S.u[0]), u00i = T(S.u[1]), u01r = T(S.u[2]), u01i = T(S.u[3]);
   const T u10r = T(S.u[4]), u10i = T(S.u[5]), u11r = T(S.u[6]), u11i = T(S.u[7]);
   const T ar = a.x, ai = a.y, br = b.x, bi = b.y;
-  a.x = fma(u00r, ar, fma(-u00i, ai, fma(u01r, br, -u01i * bi)));
-  a.y = fma(u00r, ai, fma(u00i, ar, fma(u01r, bi, u01i * br)));
-  b.x = fma(u10r, ar, fma(-u10i, ai, fma(u11r, br, -u11i * bi)));
-  b.y = fma(u10r, ai, fma(u10i, ar, fma(u11r, bi, u11i * br)));
+  if constexpr (CLS == 4) {
+    a.x = br;
+    a.y = bi;
+    b.x = ar;
+    b.y = ai;
+  } else if constexpr (CLS == 3) {
+    a.x = fma(u00r, ar, -u00i * ai);
+    a.y = fma(u00r, ai, u00i * ar);
+    b.x = fma(u11r, br, -u11i * bi);
+    b.y = fma(u11r, bi, u11i * br);
+  } else if constexpr (CLS == 2) {
+    a.x = fma(u00r, ar, -u01i * bi);
+    a.y = fma(u00r, ai, u01i * br);
+    b.x = fma(u11r, br, -u10i * ai);
+    b.y = fma(u11r, bi, u10i * ar);
+  } else if constexpr (CLS == 1) {
+    a.x = fma(u00r, ar, u01r * br);
+    a.y = fma(u00r, ai, u01r * bi);
+    b.x = fma(u10r, ar, u11r * br);
+    b.y = fma(u10r, ai, u11r * bi);
+  } else {
+    a.x = fma(u00r, ar, fma(-u00i, ai, fma(u01r, br, -u01i * bi)));
+    a.y = fma(u00r, ai, fma(u00i, ar, fma(u01r, bi, u01i * br)));
+    b.x = fma(u10r, ar, fma(-u10i, ai, fma(u11r, br, -u11i * bi)));
+    b.y = fma(u10r, ai, fma(u10i, ar, fma(u11r, bi, u11i * br)));
+  }
 }
 
 // Im(conj(x) y)
@@ -52,7 +79,7 @@ template <typename T> __device__ __forceinline__ T re_cdot(cplx_t<T> x, cplx_t<T
   return fma(x.x, y.x, x.y * y.y);
 }
 
-template <typename T>
+template <typename T, int CLS>
 __global__ void __launch_bounds__(256) adjoint_step_kernel(cplx_t<T> *__restrict__ psi,
                                                            cplx_t<T> *__restrict__ lam, uint64_t units,
                                                            const __grid_constant__ AdjStep S,
@@ -81,8 +108,8 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(cplx_t<T> *__restrict
         cnt = 0;
       }
     }
-    mv<T>(S, b0, b1);
-    mv<T>(S, a0, a1);
+    mv<T, CLS>(S, b0, b1);
+    mv<T, CLS>(S, a0, a1);
     psi[i0] = b0;
     psi[i1] = b1;
     lam[i0] = a0;
@@ -91,6 +118,18 @@ __global__ void __launch_bounds__(256) adjoint_step_kernel(cplx_t<T> *__restrict
   if (S.gen >= 0) {
     const double s = block_sum(acc + double(mini));
     if (threadIdx.x == 0) part[size_t(S.col) * nblk + blockIdx.x] = s;
+  }
+}
+
+template <typename T>
+void launch_adjoint_cls(int cls, cplx_t<T> *psi, cplx_t<T> *lam, uint64_t units, const AdjStep &S, double *d_part,
+                        int nblk, cudaStream_t s) {
+  switch (cls) {
+    case 1: adjoint_step_kernel<T, 1><<<nblk, 256, 0, s>>>(psi, lam, units, S, d_part, nblk); break;
+    case 2: adjoint_step_kernel<T, 2><<<nblk, 256, 0, s>>>(psi, lam, units, S, d_part, nblk); break;
+    case 3: adjoint_step_kernel<T, 3><<<nblk, 256, 0, s>>>(psi, lam, units, S, d_part, nblk); break;
+    case 4: adjoint_step_kernel<T, 4><<<nblk, 256, 0, s>>>(psi, lam, units, S, d_part, nblk); break;
+    default: adjoint_step_kernel<T, 0><<<nblk, 256, 0, s>>>(psi, lam, units, S, d_part, nblk); break;
   }
 }
 
@@ -126,12 +165,21 @@ cudaError_t launch_adjoint_step(int prec, void *psi, void *lam, unsigned nq, con
     if (b == g.target || ((g.ctrl_mask >> b) & 1)) S.ins[n++] = uint8_t(b);
   S.nins = n;
   const uint64_t units = uint64_t(1) << (nq - unsigned(n));
+  const double *u = S.u;  // U^dagger (re, im) x 4
+  int cls = 0;
+  if (u[0] == 0 && u[1] == 0 && u[6] == 0 && u[7] == 0 && u[2] == 1 && u[3] == 0 && u[4] == 1 && u[5] == 0)
+    cls = 4;
+  else if (u[2] == 0 && u[3] == 0 && u[4] == 0 && u[5] == 0)
+    cls = 3;
+  else if (u[1] == 0 && u[3] == 0 && u[5] == 0 && u[7] == 0)
+    cls = 1;
+  else if (u[1] == 0 && u[7] == 0 && u[2] == 0 && u[4] == 0)
+    cls = 2;
   if (prec == 1)
-    adjoint_step_kernel<float><<<nblk, 256, 0, s>>>(static_cast<float2 *>(psi), static_cast<float2 *>(lam), units, S,
-                                                    d_part, nblk);
+    launch_adjoint_cls<float>(cls, static_cast<float2 *>(psi), static_cast<float2 *>(lam), units, S, d_part, nblk, s);
   else
-    adjoint_step_kernel<double><<<nblk, 256, 0, s>>>(static_cast<double2 *>(psi), static_cast<double2 *>(lam), units,
-                                                     S, d_part, nblk);
+    launch_adjoint_cls<double>(cls, static_cast<double2 *>(psi), static_cast<double2 *>(lam), units, S, d_part, nblk,
+                               s);
   return cudaGetLastError();
 }
 
