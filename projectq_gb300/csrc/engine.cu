@@ -434,6 +434,9 @@ class Engine {
         if (!paulis_commute(terms[ks[a]], terms[ks[b]])) return false;
     std::vector<unsigned> id_at(N_, 0);
     for (auto const &kv : map_) id_at[kv.second] = kv.first;
+    std::vector<unsigned> cids;  // the controls once each (the gates' own validation rejects repeats)
+    for (unsigned c : ctrl)
+      if (std::find(cids.begin(), cids.end(), c) == cids.end()) cids.push_back(c);
     static const cplx ph[4] = {cplx(1, 0), cplx(0, -1), cplx(-1, 0), cplx(0, 1)};  // (-i)^ny
     cplx g = std::exp(cplx(0., -time * tr));
     for (size_t k : ks) {
@@ -456,7 +459,7 @@ class Engine {
           lx |= uint32_t((p.xmask >> at[i]) & 1) << i;
           lz |= uint32_t((p.sign_mask >> at[i]) & 1) << i;
         }
-        submit_gate(pauli_exp_matrix(w, lx, lz, a, b), ids, ctrl);
+        submit_gate(pauli_exp_matrix(w, lx, lz, a, b), ids, cids);
       } else {
         run();
         PauliRotationDev rd{};

@@ -276,3 +276,21 @@ def test_chebyshev_mode_identity_and_commuting():
         assert g.counters()[path] == 1
         err = float(np.max(np.abs(g.cheat()[1] - o.cheat()[1])))
         assert err <= 1e-11, err
+
+
+def test_exact_product_repeated_control_id():
+    """A control id given twice acts once (the reference ORs it into its
+    control mask)."""
+    n = 6
+    rng = np.random.default_rng(12)
+    terms = random_commuting(n - 1, 8, rng)
+    gates = random_mixed_circuit(n, 20, 9, kmax=2, max_ctrl=1)
+    g = make("gpu", seed=1, precision="c128")
+    o = make("oracle", seed=1)
+    for s in (g, o):
+        allocate(s, n)
+        run_circuit(s, gates)
+        s.emulate_time_evolution(terms, 0.9, list(range(n - 1)), [n - 1, n - 1])
+    assert g.counters()["evolutions_exact"] == 1
+    err = float(np.max(np.abs(g.cheat()[1] - o.cheat()[1])))
+    assert err <= 1e-11, err
