@@ -48,7 +48,8 @@ SIGNATURES = {
     "measure_qubits": (C.c_int, [_eng, _u32p, _sz, _u8p]),
     "measure_qubits_at": (C.c_int, [_eng, _u32p, _sz, C.c_double, _u8p]),
     "apply_gates": (C.c_int, [_eng, _sz, _u32p, _u32p, _u32p, _f64p, C.POINTER(_sz)]),
-    "apply_controlled_gate": (C.c_int, [_eng, _f64p, C.c_uint32, _u32p, _u32p, _sz]),
+    # the matrix by address (c_void_p): callers pass ndarray.ctypes.data
+    "apply_controlled_gate": (C.c_int, [_eng, C.c_void_p, C.c_uint32, _u32p, _u32p, _sz]),
     "run": (C.c_int, [_eng]),
     "emulate_math_add_constant": (C.c_int, [_eng, C.c_int32, _u32p, _u32p, _sz, _u32p, _sz]),
     "emulate_math_add_constant_modn": (

@@ -63,11 +63,13 @@ def _bits(bits) -> np.ndarray:
 def _ids(ids) -> list:
     out = []
     for i in ids:
-        if isinstance(i, bool) or not isinstance(i, numbers.Integral):
-            raise TypeError("qubit ids must be integers")
+        if type(i) is not int:  # plain ints skip the slower abstract-class checks
+            if isinstance(i, bool) or not isinstance(i, numbers.Integral):
+                raise TypeError("qubit ids must be integers")
+            i = int(i)
         if i < 0 or i > 0xFFFFFFFF:
             raise TypeError("qubit ids must fit in an unsigned 32-bit integer")
-        out.append(int(i))
+        out.append(i)
     return out
 
 
@@ -197,16 +199,21 @@ class Simulator:
         return [bool(v) for v in out]
 
     def apply_controlled_gate(self, m, ids, ctrl):
-        """simulator.hpp:204-222: queue a controlled gate (fused, run lazily)."""
+        """simulator.hpp:204-222: queue a controlled gate (fused, run lazily).
+
+        Called once per gate by ProjectQ's Simulator._handle, so the argument
+        packing is kept short: ids as ctypes arrays, the matrix by address."""
         ids = _ids(ids)
-        ctrl = _u32(_ids(ctrl))
+        ctrl = _ids(ctrl)
         mat = np.ascontiguousarray(m, dtype=np.complex128)
         k = len(ids)
         if mat.ndim != 2 or mat.shape != (1 << k, 1 << k):
             raise ValueError(f"apply_controlled_gate(): a {k}-qubit gate needs a {1 << k}x{1 << k} matrix")
-        ida = _u32(ids)
-        self._check(self._api.apply_controlled_gate(self._h, _p(mat.view(np.float64), C.c_double), k,
-                                                    _p(ida, C.c_uint32), _p(ctrl, C.c_uint32), len(ctrl)))
+        nc = len(ctrl)
+        rc = self._api.apply_controlled_gate(self._h, mat.ctypes.data, k, (C.c_uint32 * k)(*ids),
+                                             (C.c_uint32 * nc)(*ctrl), nc)
+        if rc:
+            self._check(rc)
 
     def run(self):
         """simulator.hpp:487-527: apply all pending gates."""
