@@ -82,7 +82,6 @@ struct TcArgs {
   uint64_t groups;      // number of amplitude groups
   uint64_t ctrl_set;
   int nins, k;
-  int renorm;           // U is unitary: rescale each group's outputs to its input norm
   uint8_t ins[64];
   uint64_t off[128];    // offset of amplitude j of a group (j < 2^k, k <= 7)
 };
@@ -272,7 +271,9 @@ __device__ __forceinline__ void split_store(unsigned char *st, int row, int half
   }
 }
 
-template <int KQ, bool PAIR>
+// RENORM: U is unitary and each group's outputs are rescaled to the group's
+// input norm (a compile-time choice, so the plain kernel carries none of it).
+template <int KQ, bool PAIR, bool RENORM>
 __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
     tc_gate_kernel(float2 *__restrict__ psi, const float *__restrict__ bsrc, const __grid_constant__ TcArgs A,
                    int *err) {
@@ -366,7 +367,7 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       split_store(stages + size_t(s) * Cfg::kStageBytes, row, half, x);
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       mbar_arrive(full0 + 8 * s);
-      if (A.renorm) {
+      if constexpr (RENORM) {
 #pragma unroll
         for (int q = 0; q < 8; ++q) nacc = fmaf(x[q].x, x[q].x, fmaf(x[q].y, x[q].y, nacc));
         if (int(it % NCH) == NCH - 1) {  // the tile's last chunk: hand the norm to the epilogue
@@ -413,39 +414,58 @@ __global__ void __launch_bounds__(TcCfg<KQ>::kThreads, 1)
       // 1e-8 x K relative per gate, always downwards), which for a unitary U
       // is a loss of norm; each group's outputs are rescaled to the group's
       // input norm (exact for unitary U up to FP32 rounding).
-      float scale = 1.f;
-      if (A.renorm) {
+      auto store_cols = [&](const float (&v)[EC], int c0) {
+        if (!active) return;
+        if constexpr (PAIR) {
+#pragma unroll
+          for (int q = 0; q < EC / 2; q += 2)
+            __stcs(reinterpret_cast<float4 *>(psi + base + A.off[c0 / 2 + q]),
+                   make_float4(v[2 * q], v[2 * q + 1], v[2 * q + 2], v[2 * q + 3]));
+        } else {
+#pragma unroll
+          for (int q = 0; q < EC / 2; ++q) __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
+        }
+      };
+      if constexpr (RENORM) {
         const uint32_t nb = i % Cfg::NB, nu = i / Cfg::NB;
         if (!mbar_wait(nfull0 + 8 * nb, nu & 1u, abort_flag, err)) break;
         const float s_in = nin[(nb * kRows + row) * 2] + nin[(nb * kRows + row) * 2 + 1];
         mbar_arrive(nemp0 + 8 * nb);
         float s_out = 0.f;
+        if constexpr (N == EC) {
+          // k <= 5: one TMEM load holds the row; norm, scale and store from registers
+          float v[EC];
+          tmem_ld<EC>(tmem + lane_base + b * uint32_t(N), v);
+#pragma unroll
+          for (int q = 0; q < EC; ++q) s_out = fmaf(v[q], v[q], s_out);
+          const float scale = (s_out > 0.f && s_in > 0.f) ? sqrtf(s_in / s_out) : 1.f;
+#pragma unroll
+          for (int q = 0; q < EC; ++q) v[q] *= scale;
+          store_cols(v, 0);
+        } else {
+#pragma unroll 1
+          for (int c0 = 0; c0 < N; c0 += EC) {
+            float v[EC];
+            tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+#pragma unroll
+            for (int q = 0; q < EC; ++q) s_out = fmaf(v[q], v[q], s_out);
+          }
+          const float scale = (s_out > 0.f && s_in > 0.f) ? sqrtf(s_in / s_out) : 1.f;
+#pragma unroll 1
+          for (int c0 = 0; c0 < N; c0 += EC) {
+            float v[EC];
+            tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
+#pragma unroll
+            for (int q = 0; q < EC; ++q) v[q] *= scale;
+            store_cols(v, c0);
+          }
+        }
+      } else {
 #pragma unroll 1
         for (int c0 = 0; c0 < N; c0 += EC) {
           float v[EC];
           tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
-#pragma unroll
-          for (int q = 0; q < EC; ++q) s_out = fmaf(v[q], v[q], s_out);
-        }
-        if (s_out > 0.f && s_in > 0.f) scale = sqrtf(s_in / s_out);
-      }
-#pragma unroll 1
-      for (int c0 = 0; c0 < N; c0 += EC) {
-        float v[EC];
-        tmem_ld<EC>(tmem + lane_base + b * uint32_t(N) + uint32_t(c0), v);
-#pragma unroll
-        for (int q = 0; q < EC; ++q) v[q] *= scale;
-        if (active) {
-          if constexpr (PAIR) {
-#pragma unroll
-            for (int q = 0; q < EC / 2; q += 2)
-              __stcs(reinterpret_cast<float4 *>(psi + base + A.off[c0 / 2 + q]),
-                     make_float4(v[2 * q], v[2 * q + 1], v[2 * q + 2], v[2 * q + 3]));
-          } else {
-#pragma unroll
-            for (int q = 0; q < EC / 2; ++q)
-              __stcs(psi + base + A.off[c0 / 2 + q], make_float2(v[2 * q], v[2 * q + 1]));
-          }
+          store_cols(v, c0);
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -583,17 +603,17 @@ cudaError_t launch_tc_kp(void *psi, unsigned nq, const DenseOp &op, const float 
     for (int l = 0; l < KQ; ++l)
       if ((j >> l) & 1) A.off[j] |= uint64_t(1) << op.pos[l];
   A.groups = uint64_t(1) << (nq - ins.size());
-  A.renorm = renorm && tc_is_unitary(op.m, KQ) ? 1 : 0;
+  const bool rn = renorm && tc_is_unitary(op.m, KQ);
+  auto *kern = rn ? tc_gate_kernel<KQ, PAIR, true> : tc_gate_kernel<KQ, PAIR, false>;
   // set on every launch: attributes belong to the current device
-  const cudaError_t e =
-      cudaFuncSetAttribute(tc_gate_kernel<KQ, PAIR>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::kSmem));
+  const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(Cfg::kSmem));
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 1;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const uint64_t ntiles = (A.groups + kRows - 1) / kRows;
   const unsigned grid = unsigned(std::max<uint64_t>(1, std::min<uint64_t>(ntiles, uint64_t(sms))));
-  tc_gate_kernel<KQ, PAIR><<<grid, Cfg::kThreads, Cfg::kSmem, s>>>(static_cast<float2 *>(psi), d_b, A, d_err);
+  kern<<<grid, Cfg::kThreads, Cfg::kSmem, s>>>(static_cast<float2 *>(psi), d_b, A, d_err);
   return cudaGetLastError();
 }
 
