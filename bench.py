@@ -130,10 +130,10 @@ class ClockSampler:
 
 KERNEL_KINDS = ["dense_gate", "stage", "wide_gate", "tensor_core_gate"]
 # DRAM bytes (read + write) per amplitude of one stage-kernel launch, from the
-# ncu capture of the 26-qubit complex64 circuit (537.00 MB read + 481.78 MB
+# ncu capture of the 26-qubit complex64 circuit (536.98 MB read + 481.61 MB
 # written per launch over 2^26 amplitudes); traffic grows with the state
 # size, so a 30-qubit launch moves 2^30 times this.
-NCU_TRAFFIC_PER_AMP = {(1, 1): (536.995328e6 + 481.783552e6) / 2 ** 26}
+NCU_TRAFFIC_PER_AMP = {(1, 1): (536.98432e6 + 481.609728e6) / 2 ** 26}
 NCU_TRAFFIC_SOURCE = "profiles/stage_reg_kernel_c64_26q_ncu.md, scaled from 2^26 to 2^nq amplitudes"
 
 
