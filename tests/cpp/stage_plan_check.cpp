@@ -245,3 +245,28 @@ extern "C" int stage_plan_apply(unsigned nq, unsigned L, unsigned m, unsigned r,
   g_inconsistent = false;
   return bad ? 1 : 0;
 }
+
+// Number of operations in the planned stages (after merging) and of stages.
+extern "C" int stage_plan_count_ops(unsigned nq, unsigned L, unsigned m, size_t ngates, const uint32_t *ks,
+                                    const uint32_t *targets, const uint64_t *ctrl_masks, const double *mats,
+                                    uint32_t *nops_out, uint32_t *nstages_out) {
+  std::vector<gsim::StageGate> gates(ngates);
+  size_t to = 0, mo = 0;
+  for (size_t g = 0; g < ngates; ++g) {
+    const size_t k = ks[g], d = size_t(1) << k;
+    for (size_t l = 0; l < k; ++l) gates[g].pos.push_back(targets[to++]);
+    gates[g].ctrl_mask = ctrl_masks[g];
+    gates[g].m.resize(d * d);
+    for (size_t i = 0; i < d * d; ++i, mo += 2) gates[g].m[i] = cplx(mats[mo], mats[mo + 1]);
+  }
+  gsim::StagePlanner planner(nq, L, m);
+  uint32_t nops = 0, ns = 0;
+  for (auto &st : planner.plan(gates))
+    if (st.is_stage) {
+      nops += uint32_t(st.stage.ops.size());
+      ++ns;
+    }
+  *nops_out = nops;
+  *nstages_out = ns;
+  return 0;
+}
