@@ -60,8 +60,12 @@ def parse():
     ap.add_argument("--fusion", default="staged", choices=["staged", "reference", "none"])
     ap.add_argument("--c128-steps", type=int, default=None, help="timed steps of the complex128 arm")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-gates", type=int, default=24, help="gates in the CPU baseline sample")
+    ap.add_argument("--cpu-gates", type=int, default=100, help="gates in each mode of the CPU baseline sample")
+    ap.add_argument("--ref-gates", type=int, default=8,
+                    help="--impl reference: gates per timed window (per step, in each mode)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--check-qubits", type=int, default=26,
+                    help="qubits of the accuracy check against the CPU reference engine (0: skip)")
     ap.add_argument("--only", choices=["c64", "c128"], default=None,
                     help="profiling mode: time one precision only (no accuracy, e2e or CPU legs)")
     ap.add_argument("--init", choices=["random", "zero"], default="random",
@@ -75,6 +79,8 @@ def parse():
                          "commuting Hamiltonians, exact product vs Taylor series, and a non-commuting one, "
                          "Chebyshev expansion vs Taylor series")
     ap.add_argument("--ngates", type=int, default=60, help="fused workload: gates per step")
+    ap.add_argument("--fd-params", type=int, default=0,
+                    help="adjoint workload: parameters checked by finite differences (0: every parameter)")
     return ap.parse_args()
 
 
@@ -214,28 +220,85 @@ def dominant_kernel(recs):
     return key, groups
 
 
-def cpu_baseline(gates, nq, ngates):
-    """The oracle port (OpenMP, all host threads) on the first `ngates` gates of
-    the circuit at full width, one pass per gate (the reference's run() per gate)."""
-    sys.path.insert(0, str(ROOT / "tests"))
-    from _backends import make
+class CpuEngine:
+    """The CPU implementation timed as the baseline: the reference engine
+    itself, built from ProjectQ's own simulator.hpp with the flags of its
+    setup.py (oracle/_ref/libref_sim_setup.so, made by oracle/build_ref.sh),
+    with all host threads (OMP_NUM_THREADS = cores, OMP_PROC_BIND=spread);
+    the oracle port (oracle/oracle_sim.cpp) only where that build is absent.
+    One engine of `nq` qubits is allocated once (|0...0>; its kernels' times
+    do not depend on the amplitudes) and then runs windows of the circuit in
+    the reference's two modes: one run() per gate (ProjectQ's Simulator with
+    gate_fusion=False, the default) and one run() per window (gate_fusion=True,
+    the greedy fusion of simulator.hpp:204-222)."""
 
-    threads = os.cpu_count() or 1
-    sim = make("oracle", seed=0)
-    for q in range(nq):
-        sim.allocate_qubit(q)
-    sim.set_fusion("none")
-    sample = gates[:ngates]
-    t0 = time.perf_counter()
-    for m, t, c in sample:
-        sim.apply_controlled_gate(m, t, c)
-    sim.run()
-    dt = time.perf_counter() - t0
-    nbytes = sum(2 * (1 << (nq - len(c))) * 16 for _, _, c in sample)
-    del sim
-    return {"value": len(sample) / dt, "unit": "gates/s", "cores": threads, "kind": "port",
-            "sample": f"first {len(sample)} gates of the circuit at {nq} qubits, complex128, one pass per gate",
-            "hbm_like_gbs": nbytes / dt / 1e9, "seconds": dt}
+    def __init__(self, nq):
+        sys.path.insert(0, str(ROOT / "tests"))
+        from _backends import make, ref_setup_api
+
+        self.cores = os.cpu_count() or 1
+        if ref_setup_api() is not None:
+            self.kind, self.sim = "reference", make("ref_setup", seed=0)
+            self.what = "reference engine (simulator.hpp) built with setup.py's flags"
+        else:
+            self.kind, self.sim = "port", make("oracle", seed=0)
+            self.sim.set_fusion("reference")
+            self.what = "oracle port (reference build absent)"
+        self.nq = nq
+        t0 = time.perf_counter()
+        for q in range(nq):
+            self.sim.allocate_qubit(q)
+        self.setup_seconds = time.perf_counter() - t0
+
+    def window(self, gates, start, count):
+        return [gates[(start + i) % len(gates)] for i in range(count)]
+
+    def time_per_gate(self, sample):
+        t0 = time.perf_counter()
+        for m, t, c in sample:
+            self.sim.apply_controlled_gate(m, t, c)
+            self.sim.run()
+        return time.perf_counter() - t0
+
+    def time_fused(self, sample):
+        t0 = time.perf_counter()
+        for m, t, c in sample:
+            self.sim.apply_controlled_gate(m, t, c)
+        self.sim.run()
+        return time.perf_counter() - t0
+
+    def close(self):
+        self.sim.close()
+
+
+def set_omp_env():
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.environ.setdefault("OMP_PROC_BIND", "spread")
+
+
+def cpu_nq(nq):
+    """The baseline's state size: the workload's, unless host memory cannot
+    hold its complex128 state (plus the reallocation of the last allocate)."""
+    if host_memory_gib() and host_memory_gib() < 3 * (1 << nq) * 16 / 2**30 + 8:
+        return 26
+    return nq
+
+
+def cpu_baseline(gates, nq, ngates):
+    """One bounded sample at full width: the first `ngates` gates with one
+    run() per gate, and the next `ngates` with the reference's fusion."""
+    eng = CpuEngine(nq)
+    per_gate = eng.time_per_gate(eng.window(gates, 0, ngates))
+    fused = eng.time_fused(eng.window(gates, ngates, ngates))
+    eng.close()
+    best = min(per_gate, fused)
+    nbytes = sum(2 * (1 << (nq - len(c))) * 16 for _, _, c in gates[:ngates])
+    return {"value": ngates / best, "unit": "gates/s", "cores": eng.cores, "kind": eng.kind,
+            "sample": f"{eng.what}, {nq} qubits complex128: gates 0-{ngates - 1} of the circuit with one run() per "
+                      f"gate ({ngates / per_gate:.3f} gates/s) and gates {ngates}-{2 * ngates - 1} with the "
+                      f"reference's gate fusion ({ngates / fused:.3f} gates/s); value = the faster mode",
+            "per_gate_gates_per_s": ngates / per_gate, "fused_gates_per_s": ngates / fused,
+            "hbm_like_gbs_per_gate_mode": nbytes / per_gate / 1e9, "seconds": per_gate + fused}
 
 
 def host_memory_gib():
@@ -246,35 +309,87 @@ def host_memory_gib():
 
 
 def run_reference(a):
-    """--impl reference: the CPU implementation on this machine's host cores."""
+    """--impl reference: the reference's CPU engine on this machine's host
+    cores, on the same 30-qubit circuit.  Every step times a window of
+    `--ref-gates` consecutive gates (the windows advance through the circuit,
+    so K steps time K x window gates) in both of the reference's modes; the
+    value is the faster mode's gates/s over the timed steps."""
     from projectq_gb300.workloads import config2_circuit
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    set_omp_env()
     gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
-    nq = a.qubits
-    need = 2 * (1 << nq) * 16 / 2**30 + 2
-    if host_memory_gib() and host_memory_gib() < need:
-        nq = max(20, int(math.log2(host_memory_gib() * 2**30 / 40)))
-    samples = []
-    for _ in range(a.warmup):
-        cpu_baseline(gates, nq, max(4, a.cpu_gates // 4))
-    for _ in range(a.steps):
-        samples.append(cpu_baseline(gates, nq, a.cpu_gates))
-    v = statistics.median(s["value"] for s in samples)
-    cb = dict(samples[0])
-    cb["value"] = v
+    nq = cpu_nq(a.qubits)
+    eng = CpuEngine(nq)
+    S = a.ref_gates
+    for i in range(a.warmup):
+        eng.time_per_gate(eng.window(gates, i * S, S))
+    tg, tf = [], []
+    for i in range(a.warmup, a.warmup + a.steps):
+        tg.append(eng.time_per_gate(eng.window(gates, i * S, S)))
+        tf.append(eng.time_fused(eng.window(gates, i * S, S)))
+    eng.close()
+    vg, vf = S * a.steps / sum(tg), S * a.steps / sum(tf)
+    v = max(vg, vf)
+    mode = "one run() per gate" if vg >= vf else "gate fusion"
+    sample = (f"{eng.what}, {nq} qubits complex128, {a.steps} windows of {S} consecutive gates "
+              f"({S * a.steps} gates timed per mode): one run() per gate {vg:.3f} gates/s, gate fusion "
+              f"{vf:.3f} gates/s; value = {mode}")
     print(json.dumps({
         "metric": METRIC, "impl": "reference", "value": v, "unit": "gates/s", "n_gpus": a.gpus,
-        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * a.cpu_gates / v,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1000.0 * S / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic", "config": {"workload": f"random circuit, {nq} qubits, depth {a.depth}, "
-                                                    f"{a.per_layer} gates/layer (sample of {a.cpu_gates} gates)",
+                                                    f"{a.per_layer} gates/layer ({S}-gate window per step)",
                                         "qubits": nq},
-        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_baseline": {"value": v, "unit": "gates/s", "cores": eng.cores, "kind": eng.kind, "sample": sample},
+        "modes": {"per_gate_run": vg, "gate_fusion": vf},
         "e2e": {"value": v, "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+def accuracy_vs_reference(nq, depth, per_layer, fusion):
+    """The headline circuit family at `nq` qubits (the same generator and
+    seeds, i.i.d. complex Gaussian initial state) on the GPU in complex64 and
+    complex128 with the bench's planner, and on the CPU in the reference
+    engine itself (oracle/_ref/libref_sim.so: ProjectQ's simulator.hpp with
+    its own greedy fusion; the oracle port where that build is absent).
+    Returns 1 - F and max |d psi| of each GPU state against the CPU one."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _backends import make, ref_api
+    from projectq_gb300 import Simulator
+    from projectq_gb300.workloads import config2_circuit, random_state
+
+    gates = config2_circuit(nq, depth, per_layer, seed=0)
+    psi0 = random_state(nq, seed=0, dtype=np.complex128)
+    ids = list(range(nq))
+    kind = "reference engine (simulator.hpp), its own gate fusion" if ref_api() is not None else "oracle port"
+    cpu = make("ref" if ref_api() is not None else "oracle", seed=0)
+    for q in ids:
+        cpu.allocate_qubit(q)
+    cpu.set_wavefunction(psi0, ids)
+    t0 = time.perf_counter()
+    apply_circuit(cpu, gates)
+    cpu_seconds = time.perf_counter() - t0
+    ref = cpu.cheat()[1]
+    cpu.close()
+    nref = float(np.vdot(ref, ref).real)
+    out = {"qubits": nq, "gates": len(gates), "reference": kind, "cpu_seconds": cpu_seconds}
+    for prec in ("c64", "c128"):
+        sim = Simulator(1, precision=prec, fusion=fusion)
+        for q in ids:
+            sim.allocate_qubit(q)
+        sim.set_wavefunction(psi0.astype(np.complex64) if prec == "c64" else psi0, ids)
+        apply_circuit(sim, gates)
+        st = sim.cheat()[1]
+        sim.close()
+        ip = np.vdot(ref, st)
+        out[prec] = {"one_minus_fidelity": float(1.0 - abs(ip) ** 2 / (nref * float(np.vdot(st, st).real))),
+                     "max_abs_err": float(np.max(np.abs(st - ref)))}
+        del st
+    return out
 
 
 def run_only(a):
@@ -455,15 +570,34 @@ def run_gates(a):
                       "kernels": out}), flush=True)
 
 
+def public_energy(sim, circ, theta, terms, zero):
+    """E(theta) through the plain public path, independent of the adjoint
+    kernels: set_wavefunction(|0...0>), the circuit's gates through
+    apply_gates + run (the stage planner), then get_expectation_value."""
+    ids = list(range(zero.size.bit_length() - 1))
+    sim.set_wavefunction(zero, ids)
+    sim.apply_gates(circ.gates(theta))
+    sim.run()
+    return sim.get_expectation_value(terms, ids)
+
+
 def run_adjoint(a):
     """Energy and gradient of the hardware-efficient ansatz (20 layers of Ry,
     Rz on each qubit + CNOT ladder: 960 parameters at 24 qubits) for a
-    200-term random Pauli Hamiltonian, by one adjoint sweep; checked against
-    central finite differences (h = 1e-4) and the parameter-shift rule on 8
-    parameters; plus a batch of 16 parameter sets with 4, 8, 12 and 20
-    layers (complex64)."""
+    200-term random Pauli Hamiltonian, by one adjoint sweep.  Checked (c128):
+    against central finite differences (h = 1e-4) on EVERY parameter, with
+    energies from the plain public path (public_energy: 1920 evaluations);
+    against the parameter-shift rule on 8 parameters; and the energy against
+    the reference engine itself on the CPU (simulator.hpp's
+    get_expectation_value, oracle/_ref/libref_sim.so; the oracle port where
+    that build is absent).  Plus a batch of 16 parameter sets with 4, 8, 12
+    and 20 layers (complex64).  --fd-params limits the finite differences to
+    that many evenly spaced parameters (0: all)."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from _backends import make, ref_api
     from projectq_gb300 import Simulator
     from projectq_gb300.adjoint import energy_and_gradient, hardware_efficient_ansatz
+    from projectq_gb300.simulator import pin_host
     from projectq_gb300.workloads import random_pauli_hamiltonian
 
     nq = 24 if a.qubits == 30 else a.qubits
@@ -484,28 +618,60 @@ def run_adjoint(a):
         rec = {"seconds_per_gradient": dt, "energy": e}
         if prec == "c128":
             h = 1e-4
-            idx = np.linspace(0, circ.nparams - 1, 8).astype(int)
-            fd = []
-            for j in idx:
+            # central finite differences on every parameter, energies through the public path
+            fsim = Simulator(1, precision="c128", fusion="staged")
+            for q in range(nq):
+                fsim.allocate_qubit(q)
+            zero = np.zeros(1 << nq, dtype=np.complex128)
+            zero[0] = 1.0
+            pin = pin_host(zero)
+            e_pub = public_energy(fsim, circ, theta, terms, zero)
+            idx = (np.arange(circ.nparams) if a.fd_params == 0
+                   else np.linspace(0, circ.nparams - 1, a.fd_params).astype(int))
+            t0 = time.perf_counter()
+            fd = np.empty(idx.size)
+            for i, j in enumerate(idx):
                 tp, tm = theta.copy(), theta.copy()
                 tp[j] += h
                 tm[j] -= h
-                fd.append((energy_and_gradient(sim, circ, tp, terms, range(nq))[0]
-                           - energy_and_gradient(sim, circ, tm, terms, range(nq))[0]) / (2 * h))
-            fd = np.array(fd)
-            rec["fd_max_rel_err"] = float(np.max(np.abs(g[idx] - fd)) / max(1.0, np.max(np.abs(fd))))
+                fd[i] = (public_energy(fsim, circ, tp, terms, zero) - public_energy(fsim, circ, tm, terms, zero)) / (2 * h)
+            fd_seconds = time.perf_counter() - t0
+            pin.close()
+            fsim.close()
+            err = np.abs(g[idx] - fd)
+            scale = max(1.0, float(np.max(np.abs(fd))))
+            rec["finite_differences"] = {
+                "h": h, "parameters_checked": int(idx.size), "energies": int(2 * idx.size),
+                "energy_path": "set_wavefunction + apply_gates + run + get_expectation_value (stage planner)",
+                "fd_all_max_rel_err": float(np.max(err)) / scale, "max_abs_err": float(np.max(err)),
+                "median_abs_err": float(np.median(err)), "max_abs_fd": float(np.max(np.abs(fd))),
+                "seconds": fd_seconds, "energy_public_path_minus_adjoint": e_pub - e}
             # parameter shift (exact for exp(-i theta P / 2)): (E(t + pi/2) - E(t - pi/2)) / 2
+            pidx = np.linspace(0, circ.nparams - 1, 8).astype(int)
             ps = []
-            for j in idx:
+            for j in pidx:
                 tp, tm = theta.copy(), theta.copy()
                 tp[j] += np.pi / 2
                 tm[j] -= np.pi / 2
                 ps.append((energy_and_gradient(sim, circ, tp, terms, range(nq))[0]
                            - energy_and_gradient(sim, circ, tm, terms, range(nq))[0]) / 2)
-            rec["param_shift_max_abs_err"] = float(np.max(np.abs(g[idx] - np.array(ps))))
-            g128 = g
+            rec["param_shift_max_abs_err"] = float(np.max(np.abs(g[pidx] - np.array(ps))))
+            # the energy on the CPU reference engine (FP64, its own fusion)
+            kind = "reference engine (simulator.hpp)" if ref_api() is not None else "oracle port"
+            cpu = make("ref" if ref_api() is not None else "oracle", seed=1)
+            for q in range(nq):
+                cpu.allocate_qubit(q)
+            t0 = time.perf_counter()
+            apply_circuit(cpu, circ.gates(theta))
+            e_cpu = cpu.get_expectation_value(terms, list(range(nq)))
+            cpu.close()
+            rec["energy_vs_cpu_reference"] = {"reference": kind, "energy": e_cpu, "abs_err": abs(e - e_cpu),
+                                              "seconds": time.perf_counter() - t0}
+            g128, e128 = g, e
         else:
             rec["max_abs_diff_vs_c128"] = float(np.max(np.abs(g - g128)))
+            rec["energy_abs_diff_vs_c128"] = abs(e - e128)
+            rec["energy_abs_err_vs_cpu_reference"] = abs(e - out["c128"]["energy_vs_cpu_reference"]["energy"])
             # a batch of 16 parameter sets, 4 each of 4, 8, 12 and 20 layers
             rng = np.random.default_rng(1)
             batch = []
@@ -518,6 +684,7 @@ def run_adjoint(a):
                 energy_and_gradient(sim, c, th, terms, range(nq))
             rec["batch16_seconds"] = time.perf_counter() - t0
             rec["batch16_parameters"] = int(sum(c.nparams for c, _ in batch))
+        sim.close()
         out[prec] = rec
     print(json.dumps(out), flush=True)
 
@@ -642,6 +809,7 @@ def run_evolution(a):
 
 def main():
     a = parse()
+    set_omp_env()
     if a.impl == "reference":
         run_reference(a)
         return
@@ -662,6 +830,7 @@ def main():
     gates = config2_circuit(nq, a.depth, a.per_layer, seed=0)
     G = len(gates)
     psi0 = random_state(nq, seed=0, dtype=np.complex64)
+    h2d_bytes = int(psi0.nbytes)
     ids = list(range(nq))
 
     # --- accuracy: one circuit from psi0 on both precisions ------------------
@@ -714,17 +883,19 @@ def main():
     pin.close()
     e2e = allreduce_max(dist, statistics.median(e2e_times))
 
-    # --- CPU baseline (rank 0, N = 1 only) -------------------------------------
+    # --- CPU legs (rank 0, N = 1 only): baseline, and accuracy at check size -
     cpu = None
+    vs_ref = None
     if rank == 0 and world == 1 and not a.no_cpu:
-        cq = nq
-        if host_memory_gib() and host_memory_gib() < 2 * (1 << nq) * 16 / 2**30 + 8:
-            cq = 26
+        del psi0, pin
+        s64.close()
         try:
-            cpu = cpu_baseline(gates, cq, a.cpu_gates)
+            cpu = cpu_baseline(gates, cpu_nq(nq), a.cpu_gates)
         except Exception as exc:  # pragma: no cover - host memory
             cpu = {"value": None, "unit": "gates/s", "cores": os.cpu_count(), "kind": "port",
                    "sample": f"failed: {exc}"}
+        if a.check_qubits:
+            vs_ref = accuracy_vs_reference(a.check_qubits, a.depth, a.per_layer, a.fusion)
 
     if rank != 0:
         return
@@ -767,8 +938,9 @@ def main():
         "c128": {"value": v128, "unit": "gates/s", "ms_per_step": ms128 / k128, "steps": k128,
                  "hbm_gbs": cnt128["gate_bytes"] / (ms128 * 1e-3) / 1e9},
         "c64_over_c128": value / v128,
-        "accuracy": {"one_minus_fidelity": one_minus_f, "max_abs_err": maxerr, "reference": "engine c128 path"},
-        "e2e": {"value": world * G / e2e, "unit": "gates/s", "h2d_bytes_per_step": int(psi0.nbytes),
+        "accuracy": {"one_minus_fidelity": one_minus_f, "max_abs_err": maxerr, "reference": "engine c128 path",
+                     "vs_reference": vs_ref},
+        "e2e": {"value": world * G / e2e, "unit": "gates/s", "h2d_bytes_per_step": h2d_bytes,
                 "d2h_bytes_per_step": 8 + nq, "seconds_per_step": e2e,
                 "phase_seconds_median": {k: statistics.median(p[j] for p in phases)
                                          for j, k in enumerate(("upload", "submit_and_launch", "device_expectation_measure"))},

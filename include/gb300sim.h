@@ -359,9 +359,13 @@ GSIM_API int gsim_mlp_train(void *mlp, const float *X, const float *y, int B, in
  * __device__ array that every GPU loading the library keeps until exit.
  * Limit: the summed subspace (2^(nqubits - popcount(mask)) amplitudes) may
  * hold at most 2^32 amplitudes; larger requests fail with GSIM_ERR_LENGTH.
- * The first call on a device resolves the array's address (make it before
- * any stream capture); calls that overlap on the GPU share the array and
- * race, so serialise them. */
+ * The first call on a device (and CUDA context) resolves the array's address
+ * with cudaGetSymbolAddress; with lazy module loading that first call is
+ * also when the runtime places the array, so "allocates nothing" holds from
+ * the second call on (or from the first with CUDA_MODULE_LOADING=EAGER).
+ * Make that first call before any stream capture.  The call is synchronous:
+ * it waits for `stream` and returns the result on the host.  Calls that
+ * overlap on the GPU share the array and race, so serialise them. */
 GSIM_API int gsim_probability_noalloc(const void *d_state, int precision, uint32_t nqubits,
                                       uint64_t mask, uint64_t value, double *out, void *stream);
 

@@ -78,6 +78,11 @@ class ParamCircuit:
                         5: np.diag([1.0, np.exp(1j * t)])}[k].astype(np.complex128))
         return out
 
+    def gates(self, theta):
+        """The circuit at `theta` as (2x2 matrix, [target], controls) gates for
+        apply_controlled_gate: the plain forward path, without the adjoint."""
+        return [(m, [t], list(c)) for m, t, c in zip(self.matrices(theta), self.target, self.ctrls)]
+
     def packed(self):
         off = np.zeros(len(self.kind) + 1, dtype=np.uint32)
         off[1:] = np.cumsum([len(c) for c in self.ctrls])

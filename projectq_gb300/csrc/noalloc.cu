@@ -23,9 +23,20 @@
 // systems where the GPU reaches host memory, silently reads the wrong
 // memory).  The first call on each device therefore resolves the array's
 // device address with cudaGetSymbolAddress while that device is current and
-// caches it; make that first call before any stream capture on the device.
+// caches it, keyed by the device's current CUDA context: a call under another
+// context (after cudaDeviceReset, or a caller's own driver-API context)
+// resolves it again.  That first call is also when the CUDA runtime loads
+// this file's module and places the array (lazy module loading); from then
+// on nothing is allocated.  A caller that must not see even that placement
+// makes one warm-up call (or sets CUDA_MODULE_LOADING=EAGER) first.  Make
+// the first call on a device before any stream capture on that device.
+//
+// The call is synchronous: it waits for its stream and returns the result
+// on the host.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -39,9 +50,9 @@ extern thread_local std::string g_last_error;
 
 namespace {
 
-constexpr int kMaxBlocks = 4096;
-constexpr uint64_t kPerBlock = uint64_t(1) << 20;  // amplitudes summed by one block
-constexpr uint64_t kMaxUnits = uint64_t(kMaxBlocks) * kPerBlock;  // 2^32 amplitudes
+constexpr int kMaxBlocks = 4096;                          // partial-sum slots
+constexpr uint64_t kMinPerBlock = uint64_t(1) << 14;       // amplitudes per block before the grid grows
+constexpr uint64_t kMaxUnits = uint64_t(1) << 32;          // largest summed subspace
 constexpr int kScratchDoubles = kMaxBlocks + 8;
 
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
@@ -49,6 +60,21 @@ static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double *g_addr[kMaxDevices] = {};
+CUcontext g_ctx[kMaxDevices] = {};
+
+// cuCtxGetCurrent through the runtime's driver entry point (no link to libcuda)
+using CtxGetCurrent = CUresult (*)(CUcontext *);
+CtxGetCurrent ctx_get_current() {
+  static CtxGetCurrent fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<CtxGetCurrent>(p);
+  }();
+  return fn;
+}
 
 struct Spec {
   uint8_t pos[64];
@@ -59,11 +85,11 @@ template <typename T>
 __global__ void __launch_bounds__(256) masked_norm_noalloc(const gsim::cplx_t<T> *__restrict__ psi,
                                                            uint64_t units, uint64_t val, Spec ms,
                                                            double *scratch, unsigned nblk) {
-  // Sum |psi_i|^2 over this block's share of the subspace (FP64 carried).
-  const uint64_t u0 = uint64_t(blockIdx.x) * kPerBlock;
-  const uint64_t u1 = min(units, u0 + kPerBlock);
+  // Sum |psi_i|^2 over this block's share of the subspace (grid-stride,
+  // FP64 carried); the grid is at most kMaxBlocks blocks, one slot each.
   double acc = 0.;
-  for (uint64_t u = u0 + threadIdx.x; u < u1; u += blockDim.x)
+  const uint64_t stride = uint64_t(gridDim.x) * blockDim.x;
+  for (uint64_t u = uint64_t(blockIdx.x) * blockDim.x + threadIdx.x; u < units; u += stride)
     acc += gsim::norm2_fp64(psi[gsim::insert_zeros(u, ms.pos, ms.n) | val]);
   acc = gsim::block_sum(acc);
   __shared__ bool last;
@@ -118,21 +144,25 @@ extern "C" GSIM_API int gsim_probability_noalloc(const void *d_state, int precis
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail_with(GSIM_ERR_CUDA, std::string("probability_noalloc(): no usable device: ") +
                                         cudaGetErrorString(e));
+  CUcontext ctx = nullptr;
+  if (CtxGetCurrent f = ctx_get_current()) f(&ctx);
   double *scratch = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
+    if (!g_addr[dev] || g_ctx[dev] != ctx) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p)
         return fail_with(GSIM_ERR_CUDA, std::string("probability_noalloc(): cudaGetSymbolAddress: ") +
                                             cudaGetErrorString(e));
       g_addr[dev] = static_cast<double *>(p);
+      g_ctx[dev] = ctx;
     }
     scratch = g_addr[dev];
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const unsigned nblk = unsigned((units + kPerBlock - 1) / kPerBlock);
+  // enough blocks to fill the GPU for mid-size subspaces, one scratch slot each
+  const unsigned nblk = unsigned(std::min<uint64_t>(kMaxBlocks, (units + kMinPerBlock - 1) / kMinPerBlock));
   e = cudaMemsetAsync(&scratch[kMaxBlocks], 0, sizeof(double), s);  // the counter starts at zero
   if (e == cudaSuccess) {
     if (precision == GSIM_C64)

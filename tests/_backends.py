@@ -14,6 +14,8 @@ from projectq_gb300.simulator import Simulator  # noqa: E402
 
 ORACLE_LIB = ROOT / "oracle" / "_build" / "liboracle_sim.so"
 REF_LIB = ROOT / "oracle" / "_ref" / "libref_sim.so"
+# the reference engine built with the flags of ProjectQ's setup.py (the CPU baseline)
+REF_SETUP_LIB = ROOT / "oracle" / "_ref" / "libref_sim_setup.so"
 STUBS = Path(__file__).resolve().parent / "_stubs"
 REF_PY = ROOT / "baseline" / "_ref"
 
@@ -38,6 +40,12 @@ def ref_api():
     return _cache["ref"]
 
 
+def ref_setup_api():
+    if "ref_setup" not in _cache:
+        _cache["ref_setup"] = _lib.bind(REF_SETUP_LIB, "rsim_") if REF_SETUP_LIB.exists() else None
+    return _cache["ref_setup"]
+
+
 def make(kind, seed=1, precision="c128", fusion="reference"):
     if kind == "gpu":
         return Simulator(seed, precision=precision, fusion=fusion)
@@ -45,6 +53,8 @@ def make(kind, seed=1, precision="c128", fusion="reference"):
         return Simulator(seed, fusion=fusion if fusion != "staged" else "reference", _api=oracle_api())
     if kind == "ref":
         return Simulator(seed, _api=ref_api())
+    if kind == "ref_setup":
+        return Simulator(seed, _api=ref_setup_api())
     raise ValueError(kind)
 
 

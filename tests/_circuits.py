@@ -78,3 +78,24 @@ def fma(a, b, c):
 def norm2(z):
     """|z|^2 as the reference's std::norm compiles with FMA: fma(re, re, im*im)."""
     return fma(z.real, z.real, z.imag * z.imag)
+
+
+def numpy_apply(psi, U, targets, ctrls, n):
+    """FP64 reference for one controlled k-qubit gate, independent of every
+    engine: the state as a tensor of n axes (axis a <-> bit n-1-a), the
+    target axes moved to the front in matrix-bit order (targets[k-1] first),
+    one NumPy matrix product, and the old values kept where a control is 0."""
+    k = len(targets)
+    axes = [n - 1 - q for q in reversed(targets)]
+    t = np.moveaxis(np.asarray(psi, dtype=np.complex128).reshape([2] * n), axes, list(range(k)))
+    shp = t.shape
+    X = t.reshape(1 << k, -1)
+    Y = np.asarray(U, dtype=np.complex128) @ X
+    if ctrls:
+        rest = [q for q in range(n - 1, -1, -1) if q not in targets]  # remaining axes, most significant first
+        r = np.arange(X.shape[1])
+        ok = np.ones(X.shape[1], dtype=bool)
+        for c in ctrls:
+            ok &= ((r >> (len(rest) - 1 - rest.index(c))) & 1).astype(bool)
+        Y = np.where(ok[None, :], Y, X)
+    return np.ascontiguousarray(np.moveaxis(Y.reshape(shp), list(range(k)), axes)).reshape(-1)

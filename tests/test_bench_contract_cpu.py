@@ -1,8 +1,9 @@
 """bench.py's reference arm on the CPU, at a small size: one JSON line with the
 keys the benchmark contract names (metric, value, unit, steps, warmup,
 higher_is_better, scaling, dtype, data, config, cpu_baseline, e2e with zero
-copy bytes, impl = "reference"), timed on the oracle port; and a rank other
-than 0 prints nothing."""
+copy bytes, impl = "reference"), timed on the reference engine built from its
+own sources with setup.py's flags where that build exists (else the oracle
+port); and a rank other than 0 prints nothing."""
 
 import json
 import os
@@ -17,7 +18,7 @@ def _run(extra_env=None):
     env = dict(os.environ)
     env.update(extra_env or {})
     cmd = [sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--qubits", "14", "--steps", "1",
-           "--warmup", "3", "--cpu-gates", "8"]
+           "--warmup", "3", "--ref-gates", "8"]
     return subprocess.run(cmd, cwd=str(ROOT), env=env, capture_output=True, text=True, timeout=600)
 
 
@@ -33,7 +34,9 @@ def test_reference_arm_json_line():
         assert key in d, key
     assert d["steps"] == 1 and d["warmup"] == 3 and d["higher_is_better"] is True
     assert d["value"] > 0 and d["unit"] == "gates/s"
-    assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
+    want = "reference" if (ROOT / "oracle" / "_ref" / "libref_sim_setup.so").exists() else "port"
+    assert d["cpu_baseline"]["kind"] == want and d["cpu_baseline"]["value"] == d["value"]
+    assert set(d["modes"]) == {"per_gate_run", "gate_fusion"}
     assert d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"] == {"value": d["value"], "unit": "gates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
     assert d["config"]["qubits"] == 14

@@ -28,17 +28,129 @@ def test_reference_suite_complex128(fusion):
 
 
 def test_reference_suite_complex64():
-    """complex64 storage: the reference's default pytest.approx tolerances
-    (rel 1e-6, abs 1e-12) hold except where a test compares an amplitude that
-    should be exactly zero against an absolute threshold below complex64's
-    rounding (abs=1e-12 in functional_entangle; |a| > 1e-8 after H.H in
-    test_factoring, where complex64 leaves ~3e-8); those are listed here."""
-    rc, passed, out = _refsuite.run("gpu", "c64", "staged")
-    failed = [line for line in out.splitlines() if line.startswith("FAILED")]
-    allowed = ("test_simulator_functional_entangle", "test_simulator_time_evolution", "test_factoring")
-    unexpected = [f for f in failed if not any(a in f for a in allowed)]
-    assert not unexpected, out[-6000:]
+    """complex64 storage: every test of the suite passes with the reference's
+    own tolerances, except two whose checks sit below complex64's rounding:
+    test_simulator_functional_entangle compares amplitudes that should be
+    exactly zero with pytest.approx's abs 1e-12, and test_factoring treats
+    |a| > 1e-8 as nonzero after H.H, where complex64 leaves ~3e-8.  Those two
+    are deselected here and run with stated bounds in
+    test_complex64_entangle_and_factoring_with_stated_bounds."""
+    rc, passed, out = _refsuite.run(
+        "gpu", "c64", "staged",
+        extra=["-k", "not (test_simulator_functional_entangle and cpp_simulator) "
+                     "and not (test_factoring and cpp_simulator)"])
+    assert rc == 0, out[-6000:]
     assert passed >= 50
+
+
+def _main_engine(backend_sim, engine_list=None):
+    from projectq import MainEngine
+    from projectq.backends import Simulator
+
+    backend = Simulator(gate_fusion=True)
+    backend._simulator = backend_sim
+    return MainEngine(backend, engine_list if engine_list is not None else []), backend
+
+
+def test_complex64_entangle_and_factoring_with_stated_bounds():
+    """The circuits of ProjectQ's test_simulator_functional_entangle (GHZ by
+    CNOTs, by Toffolis, uncomputed by multi-controlled X) and test_factoring
+    (Shor's order finding for N = 15, a = 2, through ProjectQ's decomposition
+    engines) in complex64, next to the same circuits on the complex128 oracle.
+    Stated bounds: every amplitude within 2e-7 of the oracle's at each
+    checkpoint, and the tests' own physical checks with "zero" meaning
+    |a| <= 1e-6 (complex64 leaves ~3e-8 where the reference expects 1e-12 or
+    1e-8)."""
+    if not projectq_available():
+        pytest.skip("ProjectQ not importable")
+    from projectq.libs.math import MultiplyByConstantModN
+    from projectq.meta import Control
+    from projectq.ops import CNOT, All, H, Measure, Toffoli, X
+    from projectq.tests._factoring_test import get_main_engine
+
+    bound, zero = 2e-7, 1e-6
+
+    def states(backends):
+        out = []
+        for b in backends:
+            mapping, vec = b.cheat()
+            out.append((mapping, np.asarray(vec, dtype=np.complex128).copy()))
+        return out
+
+    def check_close(backends):
+        (m1, v1), (m2, v2) = states(backends)
+        assert m1 == m2
+        assert np.max(np.abs(v1 - v2)) <= bound
+        return v1
+
+    # functional entangle
+    engs = [_main_engine(make("gpu", seed=1, precision="c64", fusion="staged")),
+            _main_engine(make("oracle", seed=1))]
+    regs = [e.allocate_qureg(5) for e, _ in engs]
+    for phase in range(3):
+        for (eng, _), q in zip(engs, regs):
+            if phase == 0:
+                H | q[0]
+                for qb in q[1:]:
+                    CNOT | (q[0], qb)
+            elif phase == 1:
+                for qb in q[2:]:
+                    CNOT | (q[0], qb)
+                for qb in q[2:]:
+                    Toffoli | (q[0], q[1], qb)
+            else:
+                for k in (1, 2, 3):
+                    with Control(eng, q[0:-k]):
+                        X | q[-k]
+                CNOT | (q[0], q[1])
+                H | q[0]
+            eng.flush()
+        v = check_close([b for _, b in engs])
+        if phase < 2:
+            assert abs(v[0]) ** 2 == pytest.approx(0.5, abs=zero)
+            assert abs(v[31]) ** 2 == pytest.approx(0.5, abs=zero)
+            assert np.max(np.abs(v[1:31])) <= zero
+        else:
+            assert abs(v[0]) ** 2 == pytest.approx(1.0, abs=zero)
+            assert np.max(np.abs(v[1:])) <= zero
+    for (eng, _), q in zip(engs, regs):
+        All(Measure) | q
+        eng.flush()
+
+    # factoring (N = 15, a = 2)
+    backends = [make("gpu", seed=1, precision="c64", fusion="staged"), make("oracle", seed=1)]
+    engs = [get_main_engine(_main_engine(b)[1]) for b in backends]
+    ctrls, xs = [], []
+    for eng in engs:
+        ctrls.append(eng.allocate_qubit())
+        xs.append(eng.allocate_qureg(4))
+        X | xs[-1][0]
+    for power, want_half in ((2**7, False), (2, True)):
+        for eng, c, x in zip(engs, ctrls, xs):
+            H | c
+            with Control(eng, c):
+                MultiplyByConstantModN(pow(2, power, 15), 15) | x
+            H | c
+            eng.flush()
+        sims = [e.backend for e in engs]
+        v = check_close(sims)
+        idx = sims[0].cheat()[0][ctrls[0][0].id]
+        ones = [i for i in range(len(v)) if (i >> idx) & 1]
+        if not want_half:
+            assert np.max(np.abs(v[ones])) <= zero  # the control is |0> with certainty
+        else:
+            p0 = sum(abs(v[i]) ** 2 for i in range(len(v)) if not (i >> idx) & 1 and abs(v[i]) > zero)
+            assert p0 == pytest.approx(0.5, abs=zero)
+        for eng, c in zip(engs, ctrls):
+            Measure | c
+            eng.flush()
+        if not want_half:
+            assert int(ctrls[0]) == 0
+        else:
+            break
+    for eng, x in zip(engs, xs):
+        All(Measure) | x
+        eng.flush()
 
 
 def test_reference_unitary_suite():
@@ -109,7 +221,10 @@ def test_time_evolution_against_scipy_expm(hamiltonian):
     from projectq.meta import Control
     from projectq.ops import All, H, Measure, QubitOperator, Rx, Ry, TimeEvolution
 
-    for prec, tol in (("c128", 1e-10), ("c64", 2e-5)):
+    # stated bounds on max |d psi| against expm: complex128 1e-10; complex64
+    # 1e-6 (the series runs on FP64 vectors, the exact product applies each
+    # term's exponential as a complex64 gate: a few complex64 roundings)
+    for prec, tol in (("c128", 1e-10), ("c64", 1e-6)):
         backend = Simulator(gate_fusion=True)
         backend._simulator = make("gpu", seed=1, precision=prec)
         eng = MainEngine(backend, [])
@@ -156,5 +271,5 @@ def test_time_evolution_against_scipy_expm(hamiltonian):
             Hm = Hm + c * m
         ref = scipy.sparse.linalg.expm_multiply(-1j * t * Hm, init)
         half = len(final) // 2
-        assert np.allclose(final[half:], ref / np.sqrt(2.0), atol=tol)
-        assert np.allclose(final[:half], init / np.sqrt(2.0), atol=tol)
+        assert np.max(np.abs(final[half:] - ref / np.sqrt(2.0))) <= tol
+        assert np.max(np.abs(final[:half] - init / np.sqrt(2.0))) <= tol

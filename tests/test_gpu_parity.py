@@ -408,3 +408,23 @@ def test_greedy_fusion_width(kmax):
         run_circuit(g, gates)
         run_circuit(o, gates)
         assert_states(g, o, prec, tol=TOL[prec] * (4 if prec == "c64" else 1))
+
+
+@pytest.mark.parametrize("prec", ["c64", "c128"])
+def test_cuda_array_view_is_the_engine_state(prec):
+    """Simulator.cuda_array() (the zero-copy __cuda_array_interface__ view of
+    the flushed state) consumed by torch: same dtype, shape and values as
+    cheat(), and a write through the view is seen by the engine."""
+    torch = pytest.importorskip("torch")
+    n = 12
+    sim = make("gpu", seed=1, precision=prec, fusion="staged")
+    allocate(sim, n)
+    run_circuit(sim, random_mixed_circuit(n, 60, seed=4))
+    t = torch.as_tensor(sim.cuda_array(), device="cuda")
+    assert t.dtype == (torch.complex64 if prec == "c64" else torch.complex128)
+    assert tuple(t.shape) == (1 << n,)
+    dt = np.complex64 if prec == "c64" else np.complex128
+    assert np.array_equal(t.cpu().numpy(), sim.cheat(dtype=dt)[1])
+    t[0] = 0.25 - 0.5j
+    torch.cuda.synchronize()
+    assert sim.get_amplitude([0] * n, list(range(n))) == 0.25 - 0.5j

@@ -1,6 +1,7 @@
 """Fused 4- to 7-qubit gates on complex64 states through the tcgen05
-tensor-core kernel (3xTF32, FP32 accumulation), against the complex128 path
-(FP64 arithmetic) and against complex64 on CUDA cores.  The gates are
+tensor-core kernel (3xTF32, FP32 accumulation), against an FP64 NumPy
+contraction of the same gates (tests/_circuits.py numpy_apply, independent of
+the engine), and complex64 on CUDA cores against the same.  The gates are
 Haar-random with targets spanning low and high bit positions, with and
 without controls.  Sizes cover a partial tile (fewer than 128 groups), one
 tile, and many tiles per CTA (the stage ring and both TMEM accumulators
@@ -10,7 +11,7 @@ import numpy as np
 import pytest
 
 from _backends import make
-from _circuits import allocate, haar_unitary
+from _circuits import allocate, haar_unitary, numpy_apply
 from projectq_gb300.workloads import random_state
 
 pytestmark = pytest.mark.gpu
@@ -42,7 +43,9 @@ def test_tensor_core_gates_match_fp64(k, n):
             targets = targets[::-1]  # the kernel sorts targets (and permutes U) itself
         ctrls = [int(q) for q in rest[k - 2: k - 2 + trial % 3]]
         gates.append((haar_unitary(k, rng), targets, ctrls))
-    ref = run("c128", False, n, psi, gates)
+    ref = np.asarray(psi, dtype=np.complex128)
+    for U, t, c in gates:
+        ref = numpy_apply(ref, U, t, c, n)
     tc = run("c64", True, n, psi, gates)
     cuda = run("c64", False, n, psi, gates)
     err = np.max(np.abs(tc - ref))

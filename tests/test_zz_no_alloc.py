@@ -25,9 +25,15 @@ TOL = {"c128": 1e-12, "c64": 5e-6}
 
 
 @pytest.mark.parametrize("prec", ["c128", "c64"])
-def test_probability_noalloc_matches_get_probability(prec):
+@pytest.mark.parametrize("n,patterns", [
+    # one block: summed subspaces below 2^14 amplitudes
+    (16, [([3, 9, 0], [1, 0, 1]), ([15, 2], [0, 0])]),
+    # many blocks: 2^21 and 2^19 amplitudes summed (128 and 32 blocks), so the
+    # last-block reduction and the counter reset between calls are exercised
+    (22, [([7], [1]), ([0, 21, 11], [0, 1, 1])]),
+])
+def test_probability_noalloc_matches_get_probability(prec, n, patterns):
     api = _lib.load()
-    n = 16
     sim = make("gpu", seed=1, precision=prec)
     for q in range(n):
         sim.allocate_qubit(q)
@@ -37,7 +43,7 @@ def test_probability_noalloc_matches_get_probability(prec):
     code = _lib.GSIM_C64 if prec == "c64" else _lib.GSIM_C128
     # two calls in a row, on different patterns; the scratch keeps the first
     # call's contents when the second one starts
-    for ids, bits in [([3, 9, 0], [1, 0, 1]), ([15, 2], [0, 0])]:
+    for ids, bits in patterns:
         mask = sum(1 << q for q in ids)
         value = sum(b << q for q, b in zip(ids, bits))
         out = C.c_double(-1.0)
@@ -45,6 +51,7 @@ def test_probability_noalloc_matches_get_probability(prec):
         _lib.check(api, rc)
         expected = sim.get_probability(bits, ids)
         assert out.value == pytest.approx(expected, abs=TOL[prec])
+    sim.close()
 
 
 def test_probability_noalloc_rejects_oversized_requests():
