@@ -58,6 +58,8 @@ def parse():
     ap.add_argument("--depth", type=int, default=40)
     ap.add_argument("--per-layer", type=int, default=40)
     ap.add_argument("--fusion", default="staged", choices=["staged", "reference", "none"])
+    ap.add_argument("--stage-kernel", default="packed", choices=["packed", "register", "pass"],
+                    help="stage kernel of the staged planner (complex64 packed pairs by default)")
     ap.add_argument("--c128-steps", type=int, default=None, help="timed steps of the complex128 arm")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-gates", type=int, default=100, help="gates in each mode of the CPU baseline sample")
@@ -399,6 +401,7 @@ def run_only(a):
 
     gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
     sim = Simulator(1, precision=a.only, fusion=a.fusion)
+    sim.set_stage_kernel(a.stage_kernel)
     for q in range(a.qubits):
         sim.allocate_qubit(q)
     if a.init == "random":
@@ -835,6 +838,7 @@ def main():
 
     # --- accuracy: one circuit from psi0 on both precisions ------------------
     s64 = Simulator(1, precision="c64", fusion=a.fusion)
+    s64.set_stage_kernel(a.stage_kernel)
     for q in ids:
         s64.allocate_qubit(q)
     s64.set_wavefunction(psi0, ids)

@@ -215,6 +215,13 @@ GSIM_API int gsim_set_fusion(gsim_engine *e, int mode, uint32_t kmax);
  * per gate), 2 on without that restoration. */
 GSIM_API int gsim_set_tensor_cores(gsim_engine *e, int mode);
 
+/* The stage kernel of GSIM_FUSION_STAGED: mode 2 (default) packed pairs
+ * for complex64 stages that have a tile bit none of their gates touches
+ * (amplitude pairs along that bit on packed f32x2 arithmetic; other stages
+ * and complex128 as mode 1), 1 register substages, 0 one shared-memory pass
+ * per operation.  All modes give the same results up to FP rounding. */
+GSIM_API int gsim_set_stage_kernel(gsim_engine *e, int mode);
+
 /* How emulate_time_evolution evaluates exp(-i t H): mode 1 (default) exactly,
  * as the product of exp(-i t c_k P_k) over the terms, when they commute
  * pairwise and none acts on a control (the commuting case that ProjectQ's

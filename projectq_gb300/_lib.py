@@ -106,6 +106,7 @@ PRODUCT_ONLY = {
     "reset_counters": (C.c_int, [_eng]),
     "set_device": (C.c_int, [C.c_int]),
     "set_tensor_cores": (C.c_int, [_eng, C.c_int]),
+    "set_stage_kernel": (C.c_int, [_eng, C.c_int]),
     "set_upload_mode": (C.c_int, [_eng, C.c_int]),
     "set_time_evolution": (C.c_int, [_eng, C.c_int]),
     "compare_states": (C.c_int, [_eng, _eng, _f64p]),

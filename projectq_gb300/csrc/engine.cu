@@ -813,6 +813,10 @@ class Engine {
     }
   }
   void reserve(unsigned nq) { ensure_capacity(nq); }
+  void set_stage_kernel(int mode) {
+    if (mode < 0 || mode > 2) fail(GSIM_ERR_VALUE, "stage kernel mode must be 0, 1 or 2");
+    stage_kernel_ = mode;
+  }
   void set_upload_mode(int mode) {
     if (mode != 0 && mode != 1) fail(GSIM_ERR_VALUE, "upload mode must be 0 (copy engine) or 1 (SM reads)");
     upload_mode_ = mode;
@@ -1173,7 +1177,7 @@ class Engine {
   int mode_ = GSIM_FUSION_REFERENCE;
   std::vector<QueuedGate> queue_;
   unsigned tile_bits_c64_ = kRegBitsC64 + 8, tile_bits_c128_ = kRegBitsC128 + 8;
-  bool use_reg_stages_ = true;
+  int stage_kernel_ = 2;  // 0 one pass per operation, 1 register substages, 2 packed pairs (complex64)
   bool use_tc_ = true;
   int tc_mode_ = 1;
   int te_mode_ = 1;  // emulate_time_evolution: 0 Taylor only, 1 exact for commuting terms else Taylor, 2 ... else Chebyshev
@@ -1313,12 +1317,15 @@ std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) c
   // runs of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
   const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
   const unsigned m = prec_ == GSIM_C64 ? 5 : 4;
-  StagePlanner planner(N_, L, m);
+  // complex64 stages get a pack bit where possible (the packed-pair kernel)
+  const bool pk = prec_ == GSIM_C64 && stage_kernel_ == 2;
+  StagePlanner planner(N_, L, m, 512, pk);
   std::vector<PlanStep> steps = planner.plan(gates);
   // Register substages where the tile is 2^(r + 8) amplitudes (256 threads).
   const unsigned r = prec_ == GSIM_C64 ? kRegBitsC64 : kRegBitsC128, rho = prec_ == GSIM_C64 ? 4 : 3;
   for (auto &st : steps) {
-    if (!(st.is_stage && use_reg_stages_ && st.stage.L == r + 8)) continue;
+    if (!(st.is_stage && stage_kernel_ >= 1 && st.stage.L == r + 8)) continue;
+    if (pk && build_substages_pk(st.stage)) continue;
     build_substages(st.stage, r, rho);
     if (stage_subs_bytes(st.stage) + st.stage.sops.size() * sizeof(SubOpDev) > kStageTableBytes) {
       st.stage.subs.clear();  // descriptors too large for the kernel parameter
@@ -1345,6 +1352,11 @@ void Engine::execute_staged(std::vector<PlanStep> &steps) {
     if (!steps[i].is_stage) continue;
     const StagePlan &sp = steps[i].stage;
     off_ops[i] = bytes;
+    if (!sp.pk.empty()) {  // the packed-pair blob carries its own data
+      bytes += (sp.pk.size() + 15) / 16 * 16;
+      off_pool[i] = bytes;
+      continue;
+    }
     if (!sp.subs.empty())
       bytes += stage_subs_bytes(sp) + (sp.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16;
     else
@@ -1359,6 +1371,10 @@ void Engine::execute_staged(std::vector<PlanStep> &steps) {
     for (size_t i = 0; i < steps.size(); ++i) {
       if (!steps[i].is_stage) continue;
       const StagePlan &sp = steps[i].stage;
+      if (!sp.pk.empty()) {
+        std::memcpy(host + off_ops[i], sp.pk.data(), sp.pk.size());
+        continue;
+      }
       if (!sp.subs.empty()) {
         std::memcpy(host + off_ops[i], sp.subs.data(), sp.subs.size() * sizeof(SubstageDev));
         std::memcpy(host + off_ops[i] + stage_subs_bytes(sp), sp.sops.data(), sp.sops.size() * sizeof(SubOpDev));
@@ -2144,6 +2160,9 @@ int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms) {
 }
 int gsim_set_upload_mode(gsim_engine *e, int mode) {
   return guard([&] { E(e)->set_upload_mode(mode); });
+}
+int gsim_set_stage_kernel(gsim_engine *e, int mode) {
+  return guard([&] { E(e)->set_stage_kernel(mode); });
 }
 int gsim_set_tensor_cores(gsim_engine *e, int mode) {
   return guard([&] { E(e)->set_tensor_cores(mode); });

@@ -475,6 +475,331 @@ __global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T>
   }
 }
 
+// ---- packed-pair kernel (complex64; stage.hpp: build_substages_pk) --------
+// Each thread holds 16 pairs of amplitudes as RE[jj] = (Re a, Re a'),
+// IM[jj] = (Im a, Im a'), the two amplitudes of a pair differing only in the
+// stage's pack bit, which no operation touches.  Every operation therefore
+// treats both halves alike and runs on packed f32x2 FMAs (one instruction per
+// two amplitudes).  Shared memory holds the tile as two arrays of pairs,
+// tre / tim[s(q)]; descriptors, offset tables, matrices (entries as broadcast
+// pairs (x, x), (y, y), (-y, -y)) and diagonal tables live in shared memory
+// too and are read with warp-broadcast 16-byte loads.
+namespace pk {
+
+using f2 = float2;
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+
+__device__ __forceinline__ uint32_t swz(uint32_t q) { return q ^ (((q >> 4) ^ (q >> 8)) & 15u); }
+
+// Dense 1-qubit operation on register pair-bit B; M = X00 X01 X10 X11,
+// Y00 Y01 Y10 Y11, N00 N01 N10 N11 (N = -Y), each a broadcast pair.
+template <int B, int CLS, bool MASKED>
+__device__ __forceinline__ void dense1(f2 (&RE)[16], f2 (&IM)[16], const f2 *__restrict__ M, uint32_t amask) {
+  f2 X00, X01, X10, X11, Y00, Y01, Y10, Y11, N00, N01, N10, N11;
+  X00 = M[0]; X01 = M[1]; X10 = M[2]; X11 = M[3];
+  if constexpr (CLS != 1) {
+    Y00 = M[4]; Y01 = M[5]; Y10 = M[6]; Y11 = M[7];
+    N00 = M[8]; N01 = M[9]; N10 = M[10]; N11 = M[11];
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if ((j >> B) & 1) continue;
+    constexpr int D = 1 << B;
+    const int k = j + D;
+    const f2 ar = RE[j], ai = IM[j], br = RE[k], bi = IM[k];
+    f2 a_r, a_i, b_r, b_i;
+    if constexpr (CLS == 1) {  // real
+      a_r = fma2(X00, ar, mul2(X01, br));
+      a_i = fma2(X00, ai, mul2(X01, bi));
+      b_r = fma2(X10, ar, mul2(X11, br));
+      b_i = fma2(X10, ai, mul2(X11, bi));
+    } else if constexpr (CLS == 2) {  // real diagonal, imaginary off-diagonal (Rx)
+      a_r = fma2(X00, ar, mul2(N01, bi));
+      a_i = fma2(X00, ai, mul2(Y01, br));
+      b_r = fma2(X11, br, mul2(N10, ai));
+      b_i = fma2(X11, bi, mul2(Y10, ar));
+    } else if constexpr (CLS == 4) {  // anti-diagonal
+      a_r = fma2(X01, br, mul2(N01, bi));
+      a_i = fma2(X01, bi, mul2(Y01, br));
+      b_r = fma2(X10, ar, mul2(N10, ai));
+      b_i = fma2(X10, ai, mul2(Y10, ar));
+    } else {  // general complex
+      a_r = fma2(X00, ar, fma2(N00, ai, fma2(X01, br, mul2(N01, bi))));
+      a_i = fma2(X00, ai, fma2(Y00, ar, fma2(X01, bi, mul2(Y01, br))));
+      b_r = fma2(X10, ar, fma2(N10, ai, fma2(X11, br, mul2(N11, bi))));
+      b_i = fma2(X10, ai, fma2(Y10, ar, fma2(X11, bi, mul2(Y11, br))));
+    }
+    if constexpr (MASKED) {  // pairs outside the register controls keep their values (selects, no branches)
+      const bool c = (amask >> j) & 1u;
+      RE[j] = c ? a_r : ar;
+      IM[j] = c ? a_i : ai;
+      RE[k] = c ? b_r : br;
+      IM[k] = c ? b_i : bi;
+    } else {
+      RE[j] = a_r;
+      IM[j] = a_i;
+      RE[k] = b_r;
+      IM[k] = b_i;
+    }
+  }
+}
+
+// X on register pair-bit B for the pairs in amask, as selects: the register
+// assignment stays fixed whatever the operation (a register renaming at a
+// run-time dispatch would need the same moves at every merge).
+template <int B>
+__device__ __forceinline__ void swap1(f2 (&RE)[16], f2 (&IM)[16], uint32_t amask) {
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if ((j >> B) & 1) continue;
+    const int k = j + (1 << B);
+    const bool c = (amask >> j) & 1u;
+    const f2 r0 = RE[j], i0 = IM[j], r1 = RE[k], i1 = IM[k];
+    RE[j] = c ? r1 : r0;
+    IM[j] = c ? i1 : i0;
+    RE[k] = c ? r0 : r1;
+    IM[k] = c ? i0 : i1;
+  }
+}
+
+// (RE, IM) *= F with F = Fx + i Fy per half: RE' = Fx RE - Fy IM, IM' = Fx IM + Fy RE
+__device__ __forceinline__ void cmul(f2 &re, f2 &im, f2 fx, f2 fy, f2 fn) {
+  const f2 r = re;
+  re = fma2(fx, r, mul2(fn, im));
+  im = fma2(fx, im, mul2(fy, r));
+}
+
+template <int B>
+__device__ __forceinline__ void diag1(f2 (&RE)[16], f2 (&IM)[16], const float4 *e0, const float4 *e1) {
+  const float4 a0 = e0[0], b0 = e0[1], a1 = e1[0], b1 = e1[1];
+  const f2 x0 = make_float2(a0.x, a0.y), y0 = make_float2(a0.z, a0.w), n0 = make_float2(b0.x, b0.y);
+  const f2 x1 = make_float2(a1.x, a1.y), y1 = make_float2(a1.z, a1.w), n1 = make_float2(b1.x, b1.y);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if ((j >> B) & 1) cmul(RE[j], IM[j], x1, y1, n1);
+    else cmul(RE[j], IM[j], x0, y0, n0);
+  }
+}
+
+template <int B, int CLS>
+__device__ __forceinline__ void dense1_m(f2 (&RE)[16], f2 (&IM)[16], const f2 *M, uint32_t amask, bool masked) {
+  if (masked) dense1<B, CLS, true>(RE, IM, M, amask);
+  else dense1<B, CLS, false>(RE, IM, M, amask);
+}
+
+template <int B>
+__device__ __forceinline__ void dense1_cls(f2 (&RE)[16], f2 (&IM)[16], const f2 *M, uint32_t amask, uint32_t cls,
+                                           bool masked) {
+  switch (cls) {
+    case 1: dense1_m<B, 1>(RE, IM, M, amask, masked); break;
+    case 2: dense1_m<B, 2>(RE, IM, M, amask, masked); break;
+    case 4: dense1_m<B, 4>(RE, IM, M, amask, masked); break;
+    default: dense1_m<B, 0>(RE, IM, M, amask, masked); break;
+  }
+}
+
+__device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsigned char *__restrict__ blob,
+                                         const PkOpDev &op, uint32_t code, uint32_t row, uint64_t base) {
+  const uint32_t kind = code & 15u, B = (code >> 4) & 15u;
+  if (kind == kPkDense) {
+    const f2 *M = reinterpret_cast<const f2 *>(blob + op.data);
+    const uint32_t cls = (code >> 8) & 15u;
+    const bool masked = (code >> 12) & 1u;
+    switch (B) {
+      case 0: dense1_cls<0>(RE, IM, M, op.amask, cls, masked); break;
+      case 1: dense1_cls<1>(RE, IM, M, op.amask, cls, masked); break;
+      case 2: dense1_cls<2>(RE, IM, M, op.amask, cls, masked); break;
+      default: dense1_cls<3>(RE, IM, M, op.amask, cls, masked); break;
+    }
+    return;
+  }
+  if (kind == kPkSwap) {
+    switch (B) {
+      case 0: swap1<0>(RE, IM, op.amask); break;
+      case 1: swap1<1>(RE, IM, op.amask); break;
+      case 2: swap1<2>(RE, IM, op.amask); break;
+      default: swap1<3>(RE, IM, op.amask); break;
+    }
+    return;
+  }
+  // diagonal: table index bits of the row and non-local qubits
+  uint32_t cidx = 0;
+  for (uint32_t i = 0; i < op.nsrc; ++i) {
+    const uint32_t sidx = op.src[i];
+    const uint32_t bit = (sidx & 0x80u) ? uint32_t((base >> (sidx & 0x7Fu)) & 1u) : (row >> sidx) & 1u;
+    cidx |= bit << op.sbit[i];
+  }
+  const float4 *T = reinterpret_cast<const float4 *>(blob + op.data);  // 32-byte entries
+  if (kind == kPkDiag0) {
+    const float4 a = T[2 * cidx], b = T[2 * cidx + 1];
+    const f2 x = make_float2(a.x, a.y), y = make_float2(a.z, a.w), n = make_float2(b.x, b.y);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) cmul(RE[j], IM[j], x, y, n);
+    return;
+  }
+  if (kind == kPkDiag1) {
+    const float4 *e0 = T + 2 * cidx, *e1 = T + 2 * (cidx | (1u << op.dq));
+    switch (B) {
+      case 0: diag1<0>(RE, IM, e0, e1); break;
+      case 1: diag1<1>(RE, IM, e0, e1); break;
+      case 2: diag1<2>(RE, IM, e0, e1); break;
+      default: diag1<3>(RE, IM, e0, e1); break;
+    }
+    return;
+  }
+  // several register qubits: one table entry per register index
+  const uint4 jt = *reinterpret_cast<const uint4 *>(op.jidx);
+  const uint32_t jw[4] = {jt.x, jt.y, jt.z, jt.w};
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const uint32_t idx = cidx | ((jw[j >> 2] >> (8 * (j & 3))) & 0xFFu);
+    const float4 a = T[2 * idx], b = T[2 * idx + 1];
+    cmul(RE[j], IM[j], make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y));
+  }
+}
+
+}  // namespace pk
+
+__global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ psi, const __grid_constant__ StageArgs A,
+                                                          const unsigned char *__restrict__ blob_src,
+                                                          uint32_t blob_bytes, uint32_t nsubs, uint32_t P) {
+  using pk::f2;
+  extern __shared__ __align__(16) unsigned char smem[];
+  f2 *tre = reinterpret_cast<f2 *>(smem);
+  f2 *tim = tre + 4096;
+  uint64_t *segoff = reinterpret_cast<uint64_t *>(smem + 65536);
+  const uint32_t nseg = 1u << A.h;
+  unsigned char *blob = smem + 65536 + ((nseg * 8 + 15) & ~15u);
+  for (uint32_t s = threadIdx.x; s < nseg; s += blockDim.x) {
+    uint64_t o = 0;
+    for (uint32_t b = 0; b < A.h; ++b)
+      if ((s >> b) & 1) o |= uint64_t(1) << A.lpos[A.m + b];
+    segoff[s] = o;
+  }
+  for (uint32_t i = threadIdx.x; i < blob_bytes / 16; i += blockDim.x)
+    reinterpret_cast<uint4 *>(blob)[i] = reinterpret_cast<const uint4 *>(blob_src)[i];
+  __syncthreads();
+  const PkSubDev *subs = reinterpret_cast<const PkSubDev *>(blob);
+  const PkOpDev *ops = reinterpret_cast<const PkOpDev *>(blob + ((nsubs * sizeof(PkSubDev) + 15) & ~15u));
+  const uint32_t row = threadIdx.x;
+  const uint32_t rmask = (1u << A.m) - 1;
+  for (uint64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const uint64_t base = insert_zeros(t, A.lpos, int(A.L));
+    // HBM -> shared memory: pairs along P (tile position p = q with bit P inserted)
+    if (P == 0) {
+      float4 x[16];
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint32_t p = (threadIdx.x + 256u * i) << 1;
+        x[i] = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p >> A.m] + (p & rmask)));
+      }
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint32_t sq = pk::swz(threadIdx.x + 256u * i);
+        tre[sq] = make_float2(x[i].x, x[i].z);
+        tim[sq] = make_float2(x[i].y, x[i].w);
+      }
+    } else {
+      float4 x[8], y[8];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t q = (threadIdx.x + 256u * i) << 1;
+        const uint32_t p0 = ((q >> P) << (P + 1)) | (q & ((1u << P) - 1)), p1 = p0 | (1u << P);
+        x[i] = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p0 >> A.m] + (p0 & rmask)));
+        y[i] = __ldcs(reinterpret_cast<const float4 *>(psi + base + segoff[p1 >> A.m] + (p1 & rmask)));
+      }
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t q = (threadIdx.x + 256u * i) << 1;
+        const uint32_t s0 = pk::swz(q), s1 = pk::swz(q + 1);
+        tre[s0] = make_float2(x[i].x, y[i].x);
+        tim[s0] = make_float2(x[i].y, y[i].y);
+        tre[s1] = make_float2(x[i].z, y[i].z);
+        tim[s1] = make_float2(x[i].w, y[i].w);
+      }
+    }
+    __syncthreads();
+    for (uint32_t si = 0; si < nsubs; ++si) {
+      const PkSubDev S = subs[si];
+      const uint32_t *tab = reinterpret_cast<const uint32_t *>(blob + S.tab);
+      const uint32_t srow = tab[row];
+      uint32_t o = S.op_begin;
+      uint32_t lx = 0;
+      for (; o < S.op_end; ++o) {
+        const PkOpDev &op = ops[o];
+        if (op.code != kPkLoadXor) break;
+        if ((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl) lx ^= op.amask;
+      }
+      f2 RE[16], IM[16];
+      {
+        const uint4 *lt = reinterpret_cast<const uint4 *>(tab + 256);
+        const uint32_t a0 = srow ^ lx;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const uint4 l = lt[g];
+          const uint32_t off[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const uint32_t a = a0 ^ off[e];
+            RE[4 * g + e] = tre[a];
+            IM[4 * g + e] = tim[a];
+          }
+        }
+      }
+      uint32_t sx = 0;
+      for (; o < S.op_end; ++o) {
+        const PkOpDev &op = ops[o];
+        const uint32_t code = op.code;
+        const bool on = (base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl;
+        if (code == kPkStoreXor) {
+          if (on) sx ^= op.amask;
+          continue;
+        }
+        if (!on) continue;
+        pk::apply_op(RE, IM, blob, op, code, row, base);
+      }
+      {
+        const uint4 *st = reinterpret_cast<const uint4 *>(tab + 272);
+        const uint32_t a0 = srow ^ sx;
+#pragma unroll
+        for (int g = 0; g < 4; ++g) {
+          const uint4 l = st[g];
+          const uint32_t off[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const uint32_t a = a0 ^ off[e];
+            tre[a] = RE[4 * g + e];
+            tim[a] = IM[4 * g + e];
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // shared memory -> HBM
+    if (P == 0) {
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const uint32_t q = threadIdx.x + 256u * i, p = q << 1;
+        const uint32_t sq = pk::swz(q);
+        const f2 r = tre[sq], m = tim[sq];
+        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & rmask)), make_float4(r.x, m.x, r.y, m.y));
+      }
+    } else {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const uint32_t q = (threadIdx.x + 256u * i) << 1;
+        const uint32_t p0 = ((q >> P) << (P + 1)) | (q & ((1u << P) - 1)), p1 = p0 | (1u << P);
+        const uint32_t s0 = pk::swz(q), s1 = pk::swz(q + 1);
+        const f2 r0 = tre[s0], m0 = tim[s0], r1 = tre[s1], m1 = tim[s1];
+        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p0 >> A.m] + (p0 & rmask)), make_float4(r0.x, m0.x, r1.x, m1.x));
+        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p1 >> A.m] + (p1 & rmask)), make_float4(r0.y, m0.y, r1.y, m1.y));
+      }
+    }
+    __syncthreads();
+  }
+}
+
 int stage_sms() {
   static int n = 0;
   if (!n) {
@@ -504,6 +829,26 @@ cudaError_t launch_stage_t(void *psi, unsigned nq, const StagePlan &plan, const 
   // call is cheap next to a pass over the state
   cudaError_t ae = cudaFuncSetAttribute(stage_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024);
   if (ae != cudaSuccess) return ae;
+  if constexpr (sizeof(T) == 4) {
+    if (!plan.pk.empty()) {
+      // Packed-pair substages: d_ops holds the blob (stage.hpp, build_substages_pk).
+      // runs of at least 2^5 amplitudes: 16-byte aligned loads, at most 2^8 segments
+      if (plan.L != kPkTileBits || plan.pack < 0 || A.m < 5 || plan.pk.size() % 16 || plan.pk.size() > kPkBlobMax)
+        return cudaErrorInvalidValue;
+      const size_t smem_pk = 65536 + (((size_t(1) << A.h) * 8 + 15) & ~size_t(15)) + plan.pk.size();
+      ae = cudaFuncSetAttribute(stage_pk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536 + 2048 + int(kPkBlobMax));
+      if (ae != cudaSuccess) return ae;
+      int per_sm = 1;
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, stage_pk_kernel, 256, smem_pk);
+      per_sm = std::max(1, per_sm);
+      const uint64_t grid = std::min<uint64_t>(A.ntiles, uint64_t(stage_sms()) * per_sm);
+      stage_pk_kernel<<<unsigned(grid), 256, smem_pk, s>>>(static_cast<float2 *>(psi), A,
+                                                           static_cast<const unsigned char *>(d_ops),
+                                                           uint32_t(plan.pk.size()), plan.pk_nsubs,
+                                                           uint32_t(plan.pack));
+      return cudaGetLastError();
+    }
+  }
   if (!plan.subs.empty()) {
     // Register substages: d_ops holds the table [SubstageDev...][SubOpDev...][pool].
     constexpr int R = sizeof(T) == 4 ? int(kRegBitsC64) : int(kRegBitsC128);

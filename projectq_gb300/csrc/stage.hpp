@@ -111,6 +111,9 @@ struct StagePlan {
   unsigned r = 0, rho = 0;        // register bits and bank-class bits (0: no register substages)
   std::vector<SubstageDev> subs;
   std::vector<SubOpDev> sops;
+  int pack = -1;                  // tile bit that no operation touches (packed-pair kernel), -1: none
+  std::vector<unsigned char> pk;  // packed-pair blob (build_substages_pk), empty: not used
+  uint32_t pk_nsubs = 0;
 };
 
 // Bytes of the SubstageDev array as uploaded (the SubOpDev array follows it).
@@ -350,6 +353,376 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
   }
 }
 
+// ---- packed-pair register substages (complex64) ---------------------------
+// The packed-pair stage kernel (kernels_stage.cu, stage_pk_kernel) needs a
+// tile bit P that no operation of the stage touches.  Amplitudes are held as
+// pairs along P: a "pair" q is a tile position with bit P removed (12 bits),
+// and shared memory keeps two arrays of float2, re[q] = (Re psi(q, P=0),
+// Re psi(q, P=1)) and im[q] likewise.  Every operation acts on both halves of
+// a pair identically (P is not among its qubits), so the arithmetic runs on
+// packed f32x2 FMAs.  A thread holds 16 pairs (32 amplitudes): register index
+// jj over 4 register pair-bits, and its row (0..255) over the other 8.
+// Pair positions in shared memory are swizzled, s(q) = q ^ fold4(q >> 4), so
+// pair-bit b lands in bank class b mod 4; a substage's lanes cover all four
+// classes where its register choice leaves them free.
+constexpr unsigned kPkTileBits = 13;      // 2^13 amplitudes = 4096 pairs per tile
+constexpr size_t kPkBlobMax = 40 * 1024;  // shared-memory budget for descriptors, tables and data
+
+struct PkSubDev {  // one substage
+  uint32_t op_begin, op_end;  // its operations (PkOpDev index range)
+  uint32_t tab;               // blob offset of rowtab[256], ldoff[16], stoff[16] (uint32)
+  uint32_t pad;
+};
+static_assert(sizeof(PkSubDev) == 16, "PkSubDev is read with one 16-byte load");
+
+// Operation kinds of the packed-pair kernel.
+enum : uint32_t {
+  kPkDense = 0,     // 1-qubit dense on register pair-bit b, matrix class cls
+  kPkSwap = 1,      // X on register pair-bit b (register controls in amask)
+  kPkDiag0 = 2,     // diagonal without register qubits: one factor per thread
+  kPkDiag1 = 3,     // diagonal with one register qubit (pair-bit b): two factors
+  kPkDiagN = 4,     // diagonal with several register qubits: a factor per register index
+  kPkLoadXor = 5,   // X folded into the load addresses (row / tile controls only)
+  kPkStoreXor = 6,  // X folded into the store addresses
+};
+
+struct alignas(16) PkOpDev {
+  uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12
+  uint32_t data;     // blob offset of the operation's data (16-byte aligned)
+  uint32_t amask;    // dense / swap with register controls: the register indices it pairs from (16 bits);
+                     // folded X: the address XOR
+  uint32_t tctrl;    // controls among the row bits (mask over the row index)
+  uint64_t gctrl;    // non-local controls (global bit mask)
+  uint32_t dq;       // diagonal with one register qubit: that qubit's table-index bit
+  uint32_t nsrc;     // diagonal: number of its qubits that are row bits or non-local
+  uint8_t src[8];    // those qubits: bit 7 set = non-local (bits 0-6: global position), else the row bit
+  uint8_t sbit[8];   // their table-index bits
+  uint8_t jidx[16];  // diagonal with several register qubits: table-index bits of register index jj
+};
+static_assert(sizeof(PkOpDev) == 64, "PkOpDev is read with 16-byte loads");
+
+inline uint32_t pk_swizzle(uint32_t q) { return tile_swizzle(q, 4); }
+
+// Build the packed-pair substages of a complex64 stage whose plan has a pack
+// bit (sp.pack >= 0, untouched by every operation) and only 1-qubit dense
+// operations; returns false (the stage keeps the other kernels) otherwise.
+inline bool build_substages_pk(StagePlan &sp) {
+  sp.pk.clear();
+  sp.pk_nsubs = 0;
+  if (sp.L != kPkTileBits || sp.pack < 0) return false;
+  const unsigned L = sp.L, P = unsigned(sp.pack);
+  const size_t nops = sp.ops.size();
+  for (const StageOpDev &op : sp.ops)
+    if (op.kind == 0 && op.k != 1) return false;
+  auto qbit = [&](unsigned tb) { return tb < P ? tb : tb - 1; };  // tile bit -> pair bit
+  // touched tile bits per operation (non-local qubits in gtouch), commutation as in build_substages
+  std::vector<uint32_t> ttouch(nops, 0), tmask(nops, 0);
+  std::vector<uint64_t> gtouch(nops, 0);
+  for (size_t o = 0; o < nops; ++o) {
+    const StageOpDev &op = sp.ops[o];
+    for (unsigned q = 0; q < op.k; ++q) {
+      if (op.tbit[q] == 0xFF) gtouch[o] |= uint64_t(1) << op.gbit[q];
+      else ttouch[o] |= 1u << op.tbit[q];
+    }
+    if (op.kind == 0) {
+      tmask[o] = 1u << op.tbit[0];
+      ttouch[o] |= op.lctrl;
+      gtouch[o] |= op.gctrl;
+    }
+    if ((ttouch[o] >> P) & 1) return false;  // the pack bit must be untouched
+  }
+  std::vector<std::vector<size_t>> preds(nops);
+  for (size_t b = 0; b < nops; ++b)
+    for (size_t a = 0; a < b; ++a)
+      if (((ttouch[a] & ttouch[b]) || (gtouch[a] & gtouch[b])) && !(sp.ops[a].kind == 1 && sp.ops[b].kind == 1))
+        preds[b].push_back(a);
+  struct Sub {
+    std::vector<size_t> ops;
+    uint32_t R;  // register tile bits (P included)
+  };
+  std::vector<Sub> subs;
+  std::vector<char> done(nops, 0);
+  size_t ndone = 0;
+  while (ndone < nops) {
+    uint32_t R = 1u << P;
+    std::vector<size_t> chosen;
+    bool progress = true;
+    while (progress) {
+      progress = false;
+      for (size_t o = 0; o < nops; ++o) {
+        if (done[o]) continue;
+        bool ready = true;
+        for (size_t p : preds[o])
+          if (!done[p]) {
+            ready = false;
+            break;
+          }
+        if (!ready) continue;
+        if (sp.ops[o].kind == 0) {
+          if (unsigned(__builtin_popcount(R | tmask[o])) > 5) continue;
+          R |= tmask[o];
+        }
+        done[o] = 1;
+        ++ndone;
+        chosen.push_back(o);
+        progress = true;
+      }
+    }
+    // pad to 5 register bits, from the bank classes (pair-bit mod 4) with most spare bits
+    while (unsigned(__builtin_popcount(R)) < 5) {
+      int best = -1, best_count = -1;
+      for (unsigned b = 0; b < L; ++b) {
+        if ((R >> b) & 1) continue;
+        int cnt = 0;
+        for (unsigned c = 0; c < L; ++c)
+          if (!((R >> c) & 1) && c != P && qbit(c) % 4 == qbit(b) % 4) ++cnt;
+        if (cnt > best_count) {
+          best_count = cnt;
+          best = int(b);
+        }
+      }
+      R |= 1u << best;
+    }
+    subs.push_back(Sub{chosen, R});
+  }
+  // serialise: [PkSubDev...][PkOpDev...][tables, data]
+  std::vector<PkSubDev> dsubs;
+  std::vector<PkOpDev> dops;
+  std::vector<unsigned char> data;
+  auto put = [&](const void *p, size_t n) {
+    const size_t off = data.size();
+    data.resize(off + ((n + 15) & ~size_t(15)), 0);
+    std::memcpy(data.data() + off, p, n);
+    return off;
+  };
+  // operation data shared between substages: dense matrices and diagonal tables
+  std::vector<size_t> opdata(nops, 0);
+  for (size_t o = 0; o < nops; ++o) {
+    const StageOpDev &op = sp.ops[o];
+    const cplx *M = &sp.pool[op.mat];
+    if (op.kind == 0) {
+      float d[24];  // X00 X01 X10 X11, Y.., -Y.. as broadcast pairs
+      for (int e = 0; e < 4; ++e) {
+        const float x = float(M[e].real()), y = float(M[e].imag());
+        d[2 * e] = d[2 * e + 1] = x;
+        d[8 + 2 * e] = d[8 + 2 * e + 1] = y;
+        d[16 + 2 * e] = d[16 + 2 * e + 1] = -y;
+      }
+      opdata[o] = put(d, sizeof(d));
+    } else {
+      std::vector<float> t(size_t(8) << op.k);  // entry: (fx,fx) (fy,fy) (-fy,-fy) (0,0)
+      for (size_t x = 0; x < (size_t(1) << op.k); ++x) {
+        const float fx = float(M[x].real()), fy = float(M[x].imag());
+        float *e = &t[8 * x];
+        e[0] = e[1] = fx;
+        e[2] = e[3] = fy;
+        e[4] = e[5] = -fy;
+        e[6] = e[7] = 0.f;
+      }
+      opdata[o] = put(t.data(), t.size() * sizeof(float));
+    }
+  }
+  for (const Sub &sb : subs) {
+    const uint32_t R = sb.R;
+    std::vector<unsigned> rq, rows, rest;  // register pair-bits (jj bit k), row pair-bits (row bit i)
+    std::vector<unsigned> rtile;           // register tile bits (jj bit k)
+    for (unsigned b = 0; b < L; ++b)
+      if (((R >> b) & 1) && b != P) {
+        rq.push_back(qbit(b));
+        rtile.push_back(b);
+      }
+    std::vector<char> cls(4, 0);
+    for (unsigned b = 0; b < L; ++b) {
+      if (((R >> b) & 1)) continue;
+      const unsigned qb = qbit(b);
+      if (!cls[qb % 4] && rows.size() < 4) {
+        cls[qb % 4] = 1;
+        rows.push_back(qb);
+      } else {
+        rest.push_back(qb);
+      }
+    }
+    for (unsigned qb : rest) rows.push_back(qb);
+    auto reg_of_tile = [&](unsigned tb) {
+      return int(std::find(rtile.begin(), rtile.end(), tb) - rtile.begin());
+    };
+    auto row_of_tile = [&](unsigned tb) {
+      const unsigned qb = qbit(tb);
+      return int(std::find(rows.begin(), rows.end(), qb) - rows.begin());
+    };
+    auto deposit_jj = [&](uint32_t jj) {
+      uint32_t q = 0;
+      for (unsigned k = 0; k < 4; ++k)
+        if ((jj >> k) & 1) q |= 1u << rq[k];
+      return q;
+    };
+    // each operation of the substage as a packed-pair descriptor
+    struct Cand {
+      PkOpDev d;
+      uint32_t regs;    // register bits (over jj) it touches
+      bool swap;        // an X (candidate for folding)
+      bool xor_type;    // no register controls (foldable as an address XOR)
+      uint32_t t, c;    // swap: target bit and register-control mask (over jj)
+    };
+    std::vector<Cand> cands;
+    for (size_t o : sb.ops) {
+      const StageOpDev &op = sp.ops[o];
+      Cand cd;
+      std::memset(&cd.d, 0, sizeof(cd.d));
+      cd.d.data = uint32_t(opdata[o]);
+      cd.d.gctrl = op.gctrl;
+      cd.regs = 0;
+      cd.swap = false;
+      cd.xor_type = false;
+      cd.t = cd.c = 0;
+      if (op.kind == 0) {
+        uint32_t jc = 0;
+        for (unsigned b = 0; b < L; ++b) {
+          if (!((op.lctrl >> b) & 1)) continue;
+          if ((R >> b) & 1) jc |= 1u << reg_of_tile(b);
+          else cd.d.tctrl |= 1u << row_of_tile(b);
+        }
+        const unsigned bb = unsigned(reg_of_tile(op.tbit[0]));
+        const cplx *mm = &sp.pool[op.mat];
+        const bool swap = mm[0] == cplx(0., 0.) && mm[1] == cplx(1., 0.) && mm[2] == cplx(1., 0.) &&
+                          mm[3] == cplx(0., 0.);
+        const bool real = mm[0].imag() == 0. && mm[1].imag() == 0. && mm[2].imag() == 0. && mm[3].imag() == 0.;
+        const bool rx = mm[0].imag() == 0. && mm[3].imag() == 0. && mm[1].real() == 0. && mm[2].real() == 0.;
+        const bool anti = mm[0] == cplx(0., 0.) && mm[3] == cplx(0., 0.);
+        const uint32_t cls = real ? 1 : rx ? 2 : anti ? 4 : 0;
+        for (uint32_t jj = 0; jj < 16; ++jj)
+          if (!((jj >> bb) & 1) && (jj & jc) == jc) cd.d.amask |= 1u << jj;
+        const uint32_t masked = jc ? 1u : 0u;
+        cd.d.code = (swap ? kPkSwap : kPkDense) | (bb << 4) | (cls << 8) | (masked << 12);
+        cd.regs = (1u << bb) | jc;
+        cd.swap = swap;
+        cd.xor_type = swap && jc == 0;
+        cd.t = bb;
+        cd.c = jc;
+      } else {
+        unsigned dreg = 0, dbreg = 0, dqb = 0;
+        for (unsigned q = 0; q < op.k; ++q) {
+          if (op.tbit[q] == 0xFF) {
+            cd.d.src[cd.d.nsrc] = uint8_t(0x80 | op.gbit[q]);
+            cd.d.sbit[cd.d.nsrc++] = uint8_t(q);
+          } else if ((R >> op.tbit[q]) & 1) {
+            const unsigned k = unsigned(reg_of_tile(op.tbit[q]));
+            for (uint32_t jj = 0; jj < 16; ++jj)
+              if ((jj >> k) & 1) cd.d.jidx[jj] |= uint8_t(1u << q);
+            cd.regs |= 1u << k;
+            ++dreg;
+            dbreg = k;
+            dqb = q;
+          } else {
+            cd.d.src[cd.d.nsrc] = uint8_t(row_of_tile(op.tbit[q]));
+            cd.d.sbit[cd.d.nsrc++] = uint8_t(q);
+          }
+        }
+        cd.d.dq = dqb;
+        cd.d.code = (dreg == 0 ? kPkDiag0 : dreg == 1 ? kPkDiag1 : kPkDiagN) | (dbreg << 4);
+      }
+      cands.push_back(cd);
+    }
+    // Fold X gates at the start / end of the substage into the load / store
+    // addresses: those with only row / tile controls as an address XOR,
+    // those with only register controls as a permutation of the offset table.
+    // A folded XOR moves outside the folded permutations, so it may not
+    // target a control bit of one of them.
+    const size_t nc = cands.size();
+    std::vector<char> fold(nc, 0);  // 1: front, 2: back
+    std::vector<uint32_t> perm_front(16), perm_back(16);
+    for (uint32_t jj = 0; jj < 16; ++jj) perm_front[jj] = perm_back[jj] = jj;
+    {
+      uint32_t blocked = 0, pctrl = 0;
+      for (size_t i = 0; i < nc; ++i) {
+        const Cand &cd = cands[i];
+        const bool perm_ok = cd.swap && !cd.xor_type && cd.d.tctrl == 0 && cd.d.gctrl == 0;
+        if (cd.swap && !(blocked & cd.regs) && (cd.xor_type ? !((pctrl >> cd.t) & 1) : perm_ok)) {
+          fold[i] = 1;
+          if (!cd.xor_type) {  // perm = perm o sigma
+            std::vector<uint32_t> np(16);
+            for (uint32_t jj = 0; jj < 16; ++jj) {
+              const uint32_t sj = (jj & cd.c) == cd.c ? jj ^ (1u << cd.t) : jj;
+              np[jj] = perm_front[sj];
+            }
+            perm_front = np;
+            pctrl |= cd.c;
+          }
+          continue;
+        }
+        blocked |= cd.regs;
+      }
+      blocked = 0;
+      pctrl = 0;
+      for (size_t i = nc; i-- > 0;) {
+        if (fold[i]) continue;
+        const Cand &cd = cands[i];
+        const bool perm_ok = cd.swap && !cd.xor_type && cd.d.tctrl == 0 && cd.d.gctrl == 0;
+        if (cd.swap && !(blocked & cd.regs) && (cd.xor_type ? !((pctrl >> cd.t) & 1) : perm_ok)) {
+          fold[i] = 2;
+          if (!cd.xor_type) {  // store map B^-1: perm_back = perm_back o sigma, scanning backwards
+            std::vector<uint32_t> np(16);
+            for (uint32_t jj = 0; jj < 16; ++jj) {
+              const uint32_t sj = (jj & cd.c) == cd.c ? jj ^ (1u << cd.t) : jj;
+              np[jj] = perm_back[sj];
+            }
+            perm_back = np;
+            pctrl |= cd.c;
+          }
+          continue;
+        }
+        blocked |= cd.regs;
+      }
+    }
+    PkSubDev sd;
+    std::memset(&sd, 0, sizeof(sd));
+    sd.op_begin = uint32_t(dops.size());
+    for (size_t i = 0; i < nc; ++i)
+      if (fold[i] == 1 && cands[i].xor_type) {
+        PkOpDev d = cands[i].d;
+        d.code = kPkLoadXor;
+        d.amask = pk_swizzle(1u << rq[cands[i].t]);
+        dops.push_back(d);
+      }
+    for (size_t i = 0; i < nc; ++i)
+      if (!fold[i]) dops.push_back(cands[i].d);
+    for (size_t i = nc; i-- > 0;)  // any order: XORs commute
+      if (fold[i] == 2 && cands[i].xor_type) {
+        PkOpDev d = cands[i].d;
+        d.code = kPkStoreXor;
+        d.amask = pk_swizzle(1u << rq[cands[i].t]);
+        dops.push_back(d);
+      }
+    sd.op_end = uint32_t(dops.size());
+    uint32_t tab[256 + 32];
+    for (uint32_t row = 0; row < 256; ++row) {
+      uint32_t q = 0;
+      for (unsigned i = 0; i < 8; ++i)
+        if ((row >> i) & 1) q |= 1u << rows[i];
+      tab[row] = pk_swizzle(q);
+    }
+    for (uint32_t jj = 0; jj < 16; ++jj) {
+      tab[256 + jj] = pk_swizzle(deposit_jj(perm_front[jj]));
+      tab[272 + jj] = pk_swizzle(deposit_jj(perm_back[jj]));
+    }
+    sd.tab = uint32_t(put(tab, sizeof(tab)));
+    dsubs.push_back(sd);
+  }
+  // final layout; offsets in the descriptors are made absolute
+  const size_t subs_bytes = (dsubs.size() * sizeof(PkSubDev) + 15) & ~size_t(15);
+  const size_t ops_bytes = dops.size() * sizeof(PkOpDev);
+  const size_t head = subs_bytes + ops_bytes;
+  if (head + data.size() > kPkBlobMax) return false;
+  for (PkSubDev &d : dsubs) d.tab += uint32_t(head);
+  for (PkOpDev &d : dops) d.data += uint32_t(head);
+  sp.pk.assign(head + data.size(), 0);
+  std::memcpy(sp.pk.data(), dsubs.data(), dsubs.size() * sizeof(PkSubDev));
+  std::memcpy(sp.pk.data() + subs_bytes, dops.data(), ops_bytes);
+  std::memcpy(sp.pk.data() + head, data.data(), data.size());
+  sp.pk_nsubs = uint32_t(dsubs.size());
+  return true;
+}
+
 // One step of the plan: either a stage or a single wide dense gate.
 struct PlanStep {
   bool is_stage = true;
@@ -361,8 +734,10 @@ struct PlanStep {
 class StagePlanner {
  public:
   // L: tile bits; m: contiguous low bits; window: look-ahead in gates.
-  StagePlanner(unsigned nq, unsigned L, unsigned m, size_t window = 512)
-      : nq_(nq), L_(std::min(L, nq)), m_(std::min(m, std::min(L, nq))), window_(window) {}
+  // pack: give every stage a tile bit that none of its gates touches where
+  // possible (StagePlan::pack), for the packed-pair kernel.
+  StagePlanner(unsigned nq, unsigned L, unsigned m, size_t window = 512, bool pack = false)
+      : nq_(nq), L_(std::min(L, nq)), m_(std::min(m, std::min(L, nq))), window_(window), pack_(pack) {}
 
   std::vector<PlanStep> plan(const std::vector<StageGate> &gates) const {
     // Classify every gate once.
@@ -415,7 +790,11 @@ class StagePlanner {
       PlanStep &st = steps.back();
       st.is_stage = true;
       st.ngates = uint32_t(placed.size());
-      build_stage(gates, items, placed, fill_local(local), st.stage);
+      uint64_t touched = 0;
+      for (size_t i : placed) touched |= items[i].touch;
+      const uint64_t full = pack_ ? fill_local_pack(local, touched) : fill_local(local);
+      build_stage(gates, items, placed, full, st.stage);
+      if (pack_) st.stage.pack = choose_pack(st.stage, touched);
     }
     return steps;
   }
@@ -451,6 +830,39 @@ class StagePlanner {
   uint64_t fill_local(uint64_t local) const {
     for (unsigned b = 0; b < nq_ && unsigned(__builtin_popcountll(local)) < L_; ++b) local |= uint64_t(1) << b;
     return local;
+  }
+
+  // As fill_local, but when no local bit is free of the stage's gates, the
+  // first added bit is a qubit that none of them touches (the pack bit).
+  // As fill_local, but when every local bit is used by the stage's gates,
+  // the first added bit is a qubit that none of them touches (the pack bit).
+  uint64_t fill_local_pack(uint64_t local, uint64_t touched) const {
+    if (!(local & ~touched) && unsigned(__builtin_popcountll(local)) < L_) {
+      for (unsigned b = 0; b < nq_; ++b)
+        if (!((local >> b) & 1) && !((touched >> b) & 1)) {
+          local |= uint64_t(1) << b;
+          break;
+        }
+    }
+    return fill_local(local);
+  }
+
+  // The pack bit: a tile bit no gate of the stage touches.  Preference:
+  // global bit 0 (one 16-byte load holds two whole pairs), a bit above the
+  // contiguous runs, a run bit >= 2, then bit 1 (whose pairs split each
+  // 32-byte sector between two loads).
+  int choose_pack(const StagePlan &sp, uint64_t touched) const {
+    int best = -1, best_rank = 99;
+    for (unsigned t = 0; t < sp.lpos.size(); ++t) {
+      if ((touched >> sp.lpos[t]) & 1) continue;
+      const unsigned g = sp.lpos[t];
+      const int rank = g == 0 ? 0 : g >= m_ ? 1 : g >= 2 ? 2 : 3;
+      if (rank < best_rank) {
+        best_rank = rank;
+        best = int(t);
+      }
+    }
+    return best;
   }
 
   struct Op {
@@ -612,6 +1024,7 @@ class StagePlanner {
 
   unsigned nq_, L_, m_;
   size_t window_;
+  bool pack_;
 };
 
 }  // namespace gsim

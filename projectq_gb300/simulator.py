@@ -377,6 +377,16 @@ class Simulator:
         renorm restores each amplitude group's norm after a unitary gate."""
         self._check(self._api.set_tensor_cores(self._h, (1 if renorm else 2) if on else 0))
 
+    def set_stage_kernel(self, mode="packed"):
+        """Stage kernel of the "staged" planner: "packed" (default: complex64
+        stages with a free tile bit run as amplitude pairs on packed f32x2
+        arithmetic), "register" (register substages) or "pass" (one
+        shared-memory pass per operation)."""
+        modes = {"pass": 0, "register": 1, "packed": 2}
+        if mode not in modes:
+            raise ValueError(f"stage kernel must be one of {sorted(modes)}")
+        self._check(self._api.set_stage_kernel(self._h, modes[mode]))
+
     def set_time_evolution(self, mode="exact"):
         """emulate_time_evolution: "exact" (default: the product of the terms'
         exponentials when they commute pairwise and avoid the controls, else the

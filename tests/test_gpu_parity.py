@@ -428,3 +428,28 @@ def test_cuda_array_view_is_the_engine_state(prec):
     t[0] = 0.25 - 0.5j
     torch.cuda.synchronize()
     assert sim.get_amplitude([0] * n, list(range(n))) == 0.25 - 0.5j
+
+
+@pytest.mark.parametrize("n", [14, 18, 22])
+@pytest.mark.parametrize("mode", ["packed", "register", "pass"])
+def test_stage_kernels_against_oracle(n, mode):
+    """The staged planner's three complex64 stage kernels on the headline
+    circuit family plus controlled 1-qubit gates (register, row and
+    non-local controls) against the oracle: max |d psi| 1e-5 (complex64)."""
+    from projectq_gb300.workloads import config2_circuit
+
+    gates = config2_circuit(n, depth=10, per_layer=n, seed=n)
+    rng = np.random.default_rng(n)
+    for g in random_mixed_circuit(n, 50, n + 1, kmax=1, max_ctrl=3):
+        gates.insert(int(rng.integers(len(gates) + 1)), g)
+    psi = random_state(n, seed=n)
+    g = make("gpu", seed=1, precision="c64", fusion="staged")
+    g.set_stage_kernel(mode)
+    allocate(g, n)
+    g.set_wavefunction(psi.astype(np.complex64), list(range(n)))
+    run_circuit(g, gates)
+    o = make("oracle", seed=1)
+    allocate(o, n)
+    o.set_wavefunction(psi, list(range(n)))
+    run_circuit(o, gates)
+    assert np.max(np.abs(g.cheat()[1] - o.cheat()[1])) < 1e-5

@@ -123,3 +123,94 @@ def test_lookback_merging(lib, case, r, rho):
     psi = random_state(n, seed=40 + case)
     got, _ = plan_apply(lib, n, 7, 3, gates, psi, r, rho)
     assert np.max(np.abs(got - oracle_apply(n, gates, psi))) < 1e-12
+
+
+def plan_apply_pk(lib, n, gates, psi):
+    ks = np.array([len(t) for _, t, _ in gates], dtype=np.uint32)
+    tg = np.array([q for _, t, _ in gates for q in t], dtype=np.uint32)
+    cm = np.array([sum(1 << c for c in cs) for _, _, cs in gates], dtype=np.uint64)
+    mats = np.concatenate([np.ascontiguousarray(m, dtype=np.complex128).reshape(-1) for m, _, _ in gates]).view(np.float64)
+    st = np.ascontiguousarray(psi, dtype=np.complex128).copy()
+    ns, npk = C.c_uint32(), C.c_uint32()
+    kinds = np.zeros(3, dtype=np.uint32)
+    P = lambda a, t: a.ctypes.data_as(C.POINTER(t))  # noqa: E731
+    rc = lib.stage_plan_apply_pk(C.c_uint(n), C.c_size_t(len(gates)), P(ks, C.c_uint32), P(tg, C.c_uint32),
+                                 P(cm, C.c_uint64), P(mats, C.c_double), P(st.view(np.float64), C.c_double),
+                                 C.byref(ns), C.byref(npk), P(kinds, C.c_uint32))
+    assert rc == 0, "packed-pair descriptors are inconsistent"
+    return st, ns.value, npk.value, kinds
+
+
+def _sprinkle(gates, extra, seed):
+    rng = np.random.default_rng(seed)
+    for g in extra:
+        gates.insert(int(rng.integers(len(gates) + 1)), g)
+    return gates
+
+
+@pytest.mark.parametrize("n,seed,avoid,kind,dense2", [
+    (16, 0, (0,), 0, True),          # qubit 0 left free: pairs along global bit 0
+    (18, 1, (0, 17), None, True),    # free qubits 0 and 17
+    (18, 2, (15,), None, True),      # qubits 0-4 all used
+    (13, 3, (3,), 1, False),         # the whole state is one tile; the free qubit is inside the runs
+    (20, 4, (), None, True),         # nothing left free by construction
+])
+def test_packed_pair_stages_equal_gate_by_gate(lib, n, seed, avoid, kind, dense2):
+    """The complex64 planning path: stages with a pack bit executed with the
+    packed-pair kernel's semantics (pairs along the pack bit, folded X gates as
+    address XORs and offset-table permutations, FP32 matrices and diagonal
+    tables), the rest with the register-substage kernel's; against the
+    oracle's gate-by-gate application.  The circuits mix the headline gate
+    set with controlled 1-qubit gates (register, row and non-local controls)
+    and a few 2-qubit dense gates (whose stages keep the register-substage
+    kernel); `avoid` lists qubits no gate touches, which
+    steers the pack bit to global bit 0, inside or above the contiguous runs.
+    Tolerance 2e-6 (FP32 gate data)."""
+    keep = [q for q in range(n) if q not in avoid]
+    relabel = lambda gs: [(m, tuple(keep[q] for q in t), tuple(keep[q] for q in c)) for m, t, c in gs]  # noqa: E731
+    k = len(keep)
+    # (a one-tile state holds the whole circuit in one stage: kept small enough
+    # for the kernel's shared-memory budget)
+    gates = relabel(config2_circuit(k, depth=12 if n > 13 else 4, per_layer=k, seed=seed))
+    gates = _sprinkle(gates, relabel(random_mixed_circuit(k, 60 if n > 13 else 20, seed + 10, kmax=1, max_ctrl=3)),
+                      seed)
+    if dense2:
+        gates = _sprinkle(gates, relabel(random_mixed_circuit(k, 4, seed + 20, kmax=2, max_ctrl=1)), seed + 1)
+    psi = random_state(n, seed=seed)
+    got, nst, npk, kinds = plan_apply_pk(lib, n, gates, psi)
+    exp = oracle_apply(n, gates, psi)
+    assert np.max(np.abs(got - exp)) < 2e-6
+    if avoid:
+        assert npk >= max(1, nst // 2), (npk, nst)
+    if kind is not None:
+        assert kinds[kind] >= 1, kinds
+
+
+def test_packed_pair_stage_with_pack_bit_above_the_runs(lib):
+    """Dense gates only on qubits 0-9, diagonal gates and controls on every
+    qubit but 18: each stage's dense targets leave room in the tile, and the
+    planner adds the free qubit 18 as the pack bit (pairs split across two
+    16-byte loads from different runs)."""
+    n = 20
+    rng = np.random.default_rng(7)
+    from projectq_gb300.workloads import Rx, Rz, S, T as Tg
+    others = [q for q in range(n) if q != 18]
+    gates = []
+    for _ in range(90):  # one stage (all dense targets are local), within the shared-memory budget
+        kind = int(rng.integers(5))
+        if kind == 0:
+            gates.append((H, (int(rng.integers(10)),), ()))
+        elif kind == 1:
+            gates.append((Rx(float(rng.uniform(0, 6.3))), (int(rng.integers(10)),), ()))
+        elif kind == 2:
+            t, c = (int(v) for v in rng.choice(others, 2, replace=False))
+            gates.append((X, (int(t % 10),), (c,) if c != t % 10 else ()))
+        elif kind == 3:
+            gates.append(([Tg, S, Rz(float(rng.uniform(0, 6.3)))][int(rng.integers(3))], (int(rng.choice(others)),), ()))
+        else:
+            a, b = (int(v) for v in rng.choice(others, 2, replace=False))
+            gates.append((Z, (a,), (b,)))
+    psi = random_state(n, seed=7)
+    got, nst, npk, kinds = plan_apply_pk(lib, n, gates, psi)
+    assert np.max(np.abs(got - oracle_apply(n, gates, psi))) < 2e-6
+    assert kinds[2] >= 1, kinds
