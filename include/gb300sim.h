@@ -270,12 +270,16 @@ GSIM_API int gsim_timer_mark(gsim_engine *e, int slot);
 GSIM_API int gsim_timer_elapsed(gsim_engine *e, int a, int b, float *ms);
 
 /* Per-launch profile of gate kernels: when enabled, every gate-kernel launch
- * is bracketed by CUDA events on the engine's stream.  fetch waits for the
+ * (and every step launch of a non-commuting time evolution) is bracketed by
+ * CUDA events on the engine's stream.  fetch waits for the
  * stream and copies up to cap records. */
 typedef struct gsim_launch_record {
   uint32_t kind;      /* 0 dense gate kernel (CUDA cores, k <= 5), 1 stage kernel,
-                         2 wide gate kernel (k = 6, 7), 3 tensor-core gate kernel */
-  uint32_t k;         /* matrix qubits (stage kernel: operations in the stage) */
+                         2 wide gate kernel (k = 6, 7), 3 tensor-core gate kernel,
+                         4 Taylor-series step and 5 Chebyshev step of
+                         emulate_time_evolution (non-commuting terms) */
+  uint32_t k;         /* matrix qubits (stage kernel: operations in the stage;
+                         evolution steps: Pauli terms) */
   uint32_t nctrl;     /* control qubits */
   uint32_t nqubits;   /* state qubits */
   uint64_t targets;   /* bit mask of the matrix qubits' positions */
@@ -283,7 +287,8 @@ typedef struct gsim_launch_record {
   uint32_t precision; /* GSIM_C128 or GSIM_C64 */
   uint32_t ngates;    /* logical gates applied by the launch */
   float ms;           /* device time of the launch */
-  uint32_t aux;       /* stage kernel: register substages (0: one pass per operation) */
+  uint32_t aux;       /* stage kernel: register substages (0: one pass per operation),
+                         | 1 << 16 for the packed-pair kernel */
 } gsim_launch_record;
 GSIM_API int gsim_profile_enable(gsim_engine *e, int on);
 GSIM_API int gsim_profile_fetch(gsim_engine *e, gsim_launch_record *out, size_t cap, size_t *n);
@@ -315,15 +320,18 @@ GSIM_API int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *k
                                    double *energy, double *grad);
 
 /* ---- Learned fusion planner (no reference counterpart) ----------------------
- * The cost model predicts log(milliseconds) of one kernel launch from 16
+ * The cost model predicts log(milliseconds) of one kernel launch from 20
  * features of it; GSIM_FUSION_LEARNED sums the predictions over three
  * candidate plans of the queued gates (the greedy fixed-size clusters of
  * the reference's rule, clusters whose boundaries the model chooses, the
- * stage plan) and runs the cheapest.
+ * stage plan) and runs the cheapest.  It also chooses, for each
+ * emulate_time_evolution of non-commuting terms, between the reference's
+ * Taylor series and the Chebyshev expansion by the predicted step times
+ * times the step counts (gsim_get_counters reports which ran).
  * gsim_launch_features: the features of n launch records (out: n x nfeat,
- * nfeat >= 16), the same function the planner applies to candidate launches;
+ * nfeat >= 20), the same function the planner applies to candidate launches;
  * needs no engine and no GPU.
- * gsim_set_cost_model: install trained weights (nfeatures = 16, `hidden`
+ * gsim_set_cost_model: install trained weights (nfeatures = 20, `hidden`
  * units per layer, layout of gsim_mlp_get_params).
  * gsim_set_learned_regimes: allowed[n] != 0 lets learned plans run on
  * n-qubit states (n < count <= 65); elsewhere, and without a cost model, the
@@ -337,7 +345,7 @@ GSIM_API int gsim_set_cost_model(gsim_engine *e, int nfeatures, int hidden, cons
 GSIM_API int gsim_set_learned_regimes(gsim_engine *e, const uint8_t *allowed, size_t count);
 GSIM_API int gsim_last_plan_choice(gsim_engine *e, int *mode, double *pred_ms);
 /* The planner's own evaluation of the installed network (host FP32, the same
- * arithmetic as gsim_mlp_predict's kernel) on n feature rows of 16. */
+ * arithmetic as gsim_mlp_predict's kernel) on n feature rows of 20. */
 GSIM_API int gsim_cost_model_predict(gsim_engine *e, const float *features, size_t n, float *out);
 
 /* The cost model's network: F inputs -> H -> H -> 1 (ReLU), FP32, with

@@ -1,11 +1,12 @@
 """Learned fusion cost model.
 
-A 16 -> 64 -> 64 -> 1 ReLU MLP (hand-written CUDA forward / backward / Adam
-kernels, mlp.cu) predicts log(milliseconds) of ONE kernel launch from 16
+A 20 -> 64 -> 64 -> 1 ReLU MLP (hand-written CUDA forward / backward / Adam
+kernels, mlp.cu) predicts log(milliseconds) of ONE kernel launch from 20
 features of it (gsim_launch_features: kernel kind, targets k, controls,
 lowest target bit, targets inside a 128-byte line, bytes, flops, stage
-operations and substages, state size, whether the state fits in L2,
-precision).  It is trained on the per-launch timings the engine records with
+operations and substages, packed-pair stage kernel, state size, whether the
+state fits in L2, precision, and for the steps of a non-commuting time
+evolution, series or expansion and the number of terms).  It is trained on the per-launch timings the engine records with
 its profiler while running random circuits under several planners (greedy
 fixed-size clusters of width 2..7, one launch per gate, stage plans).
 
@@ -40,7 +41,7 @@ from . import _lib
 from .simulator import Simulator
 from .workloads import Rz, Rx, Ry, X, Z, random_pauli_hamiltonian
 
-F = 16
+F = 20
 H = 64
 DATA = Path(__file__).resolve().parent / "data" / "cost_model.npz"
 # planners whose launches make up the training set: (fusion mode, kmax); the
@@ -155,7 +156,7 @@ def blocked_circuit(rng, n, block, per_block):
 
 
 def launch_features(records, api=None):
-    """Features (n x 16) of launch records (dicts of profile_records or
+    """Features (n x 20) of launch records (dicts of profile_records or
     LaunchRecord structs), computed by the engine's own gsim_launch_features."""
     api = api or _lib.load()
     n = len(records)
@@ -188,11 +189,38 @@ def record_launches(n, gates, fusion, kmax=0, precision="c64"):
     return recs
 
 
-def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64", "c128")):
+def record_evolution_launches(n, terms, t, mode, precision="c64"):
+    """The step launches of one emulate_time_evolution of `terms` (Pauli
+    terms with real coefficients, no identity) on an n-qubit |+...+> state,
+    with the series ("taylor") or the expansion ("chebyshev")."""
+    sim = _new_sim(n, precision, "staged")
+    sim.set_time_evolution(mode)
+    h = np.array([[1, 1], [1, -1]]) / np.sqrt(2.0)
+    sim.apply_gates([(h, (q,), ()) for q in range(n)])
+    sim.run()
+    sim.profile(True)
+    sim.emulate_time_evolution(terms, t, list(range(n)), [])
+    recs = [r for r in sim.profile_records() if r["kind"] in (4, 5)]
+    sim.close()
+    return recs
+
+
+def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64", "c128"), te_every=3,
+            te_nmax=26):
     """Per-launch training set: features and log(ms) of every launch of
-    `ncirc` random circuits, each run under every planner of COLLECT_PLANNERS."""
+    `ncirc` random circuits, each run under every planner of COLLECT_PLANNERS;
+    every `te_every`-th circuit also gives the step launches of a time
+    evolution of a random 10-80-term Hamiltonian, by the series and by the
+    expansion (short times: a step's cost does not depend on t, only the
+    number of steps does)."""
     rng = np.random.default_rng(seed)
     feats, ys = [], []
+
+    def add(recs):
+        if recs:
+            feats.append(launch_features(recs))
+            ys.append(np.log(np.maximum(np.array([r["ms"] for r in recs], dtype=np.float64), 1e-4)))
+
     for i in range(ncirc):
         n = int(rng.integers(nmin, nmax + 1))
         prec = precisions[i % len(precisions)]
@@ -201,9 +229,13 @@ def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64
         depth = int(rng.integers(dmin, dmax + 1))
         gates = random_circuit(rng, n, depth)
         for fusion, kmax in COLLECT_PLANNERS[prec]:
-            recs = record_launches(n, gates, fusion, kmax, prec)
-            feats.append(launch_features(recs))
-            ys.append(np.log(np.maximum(np.array([r["ms"] for r in recs], dtype=np.float64), 1e-4)))
+            add(record_launches(n, gates, fusion, kmax, prec))
+        if te_every and i % te_every == 0:
+            m = min(n, te_nmax)
+            ham = random_pauli_hamiltonian(m, nterms=int(rng.integers(10, 81)), seed=int(rng.integers(1 << 30)))
+            terms = [(tuple(tt), c) for tt, c in ham if tt]
+            for mode in ("taylor", "chebyshev"):
+                add(record_evolution_launches(m, terms, 0.05, mode, prec))
     return np.concatenate(feats), np.concatenate(ys).astype(np.float32)
 
 
@@ -273,6 +305,8 @@ def wall_time(n, gates, fusion, precision="c64", params=None, regimes=None, tail
     sim.synchronize()
     dt = time.perf_counter() - t0
     choice = last_choice(sim)[0] if fusion == "learned" else None
+    if parts is not None and tail is not None:
+        parts["tail_method"] = "chebyshev" if sim.counters()["evolutions_chebyshev"] else "taylor"
     if keep:
         return dt, choice, sim
     sim.close()
@@ -331,6 +365,8 @@ def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=30, dmin=10, dmax=200
         row = {"n": n, "gates": len(gates), "tail": tail is not None, "greedy_s": tg, "learned_s": tl,
                "greedy_gates_s": pg["gates_s"], "learned_gates_s": pl["gates_s"],
                "choice": CHOICES.get(choice, str(choice))}
+        if tail is not None:
+            row["tail_method"] = pl.get("tail_method")
         if fidelity:
             ip, err = sg.compare(sl)
             n1, n2 = sg.compare(sg)[0].real, sl.compare(sl)[0].real

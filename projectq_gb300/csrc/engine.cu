@@ -493,7 +493,6 @@ class Engine {
     uint64_t cm = 0;
     for (unsigned c : ctrl) cm |= uint64_t(1) << pos_of(c);
     if (te_mode_ >= 1 && evolve_commuting(terms, coeffs, time, ctrl, cm)) return;
-    counters_[te_mode_ == 2 ? 6 : 5] += 1;
     double tr = 0., op_nrm = 0.;
     std::vector<PauliRealTermDev> dev;
     for (size_t t = 0; t < terms.size(); ++t) {
@@ -510,6 +509,11 @@ class Engine {
     const unsigned s = unsigned(std::abs(time) * op_nrm + 1.);
     const cplx I(0., 1.);
     const cplx corr = std::exp(-time * I * tr / double(s));
+    // Chebyshev where configured, or where the learned planner's cost model
+    // predicts it faster than the series (both reach the series' accuracy)
+    const bool cheb = te_mode_ == 2 || (te_mode_ == 1 && mode_ == GSIM_FUSION_LEARNED && !cm_.empty() &&
+                                        chebyshev_predicted_faster(int(dev.size()), s, time, op_nrm, cm));
+    counters_[cheb ? 6 : 5] += 1;
     const size_t n = size_t(1) << N_;
     auto *vec = static_cast<double2 *>(aux1_.get(n * 16));
     auto *nxt = static_cast<double2 *>(aux2_.get(n * 16));
@@ -518,7 +522,7 @@ class Engine {
     auto *d_terms = static_cast<PauliRealTermDev *>(aux3_.get(std::max<size_t>(1, dev.size()) * sizeof(PauliRealTermDev)));
     if (!dev.empty())
       CK(cudaMemcpyAsync(d_terms, dev.data(), dev.size() * sizeof(dev[0]), cudaMemcpyHostToDevice, stream_));
-    if (te_mode_ == 2) {
+    if (cheb) {
       evolve_chebyshev(vec, nxt, out, d_terms, int(dev.size()), op_nrm, time, tr, cm);
     } else {
       CK(cudaMemcpyAsync(out, vec, n * 16, cudaMemcpyDeviceToDevice, stream_));
@@ -542,8 +546,10 @@ class Engine {
       double nrm_change = 1.;
       for (unsigned k = 0; nrm_change > 1.e-12; ++k) {
         const cplx coeff = (-time * I) / double(s * (k + 1));
+        const int e0 = profiling_ ? record_event() : -1;
         CK(launch_taylor_step(vec, nxt, out, N_, d_terms, nterms, coeff.real(), coeff.imag(),
                               cm, part(), d_norm, stream_));
+        if (profiling_) profile_evolution_step(4, nterms, cm, e0);
         std::swap(vec, nxt);
         double h = 0.;
         CK(cudaMemcpyAsync(&h, d_norm, 8, cudaMemcpyDeviceToHost, stream_));
@@ -575,12 +581,61 @@ class Engine {
     for (size_t k = 1; k < J.size(); ++k) {
       const cplx a = 2. * J[k] * mi[k & 3];
       // k = 1: other <- A u_0; k >= 2: other (holding u_{k-2}) <- 2 A u_{k-1} - u_{k-2}
+      const int e0 = profiling_ ? record_event() : -1;
       CK(launch_chebyshev_step(cur, other, out, N_, d_terms, nterms, (k == 1 ? 1. : 2.) / beta, k >= 2,
                                a.real(), a.imag(), cm, stream_));
+      if (profiling_) profile_evolution_step(5, nterms, cm, e0);
       std::swap(cur, other);
     }
     const cplx corr = std::exp(cplx(0., -time * tr));
     CK(launch_phase_ctrl(out, vec, n, cm, corr.real(), corr.imag(), stream_));
+  }
+
+  // Profiler record of one Taylor-series (kind 4) or Chebyshev (kind 5) step
+  // launch: k = terms; bytes = (terms + 1) complex128 vectors.
+  void profile_evolution_step(uint32_t kind, int nterms, uint64_t cm, int e0) {
+    const int e1 = record_event();
+    Prof p;
+    std::memset(&p.rec, 0, sizeof(p.rec));
+    p.rec.kind = kind;
+    p.rec.k = uint32_t(nterms);
+    p.rec.nctrl = uint32_t(__builtin_popcountll(cm));
+    p.rec.nqubits = N_;
+    p.rec.bytes = uint64_t(nterms + 1) * (uint64_t(1) << N_) * 16;
+    p.rec.precision = uint32_t(prec_);
+    p.ev0 = e0;
+    p.ev1 = e1;
+    prof_.push_back(p);
+  }
+
+  // The learned planner's choice between the reference's Taylor series and
+  // the Chebyshev expansion for one non-commuting evolution: predicted step
+  // times times step counts.  The series takes s steps of K orders each, K
+  // the first order whose term x^K / K! (x = |t| sum|c| / s) drops below the
+  // 1e-12 stop (an upper bound of the update's norm), plus a host round trip
+  // per order for that stop; the expansion takes as many steps as it has
+  // Bessel coefficients.
+  static constexpr double kOrderRoundTripMs = 0.03;  // the series' host read of each order's norm
+  static constexpr double kStepGapMs = 0.002;         // host launch gap per expansion step
+  bool chebyshev_predicted_faster(int nterms, unsigned s, double time, double op_nrm, uint64_t cm) {
+    const double x = std::abs(time) * op_nrm / double(s);
+    unsigned K = 1;
+    for (double term = x; term > 1e-12 && K < 60; ++K) term *= x / double(K + 1);
+    const size_t ncheb = bessel_j_orders(std::abs(time * op_nrm), 1e-16).size();
+    gsim_launch_record r;
+    std::memset(&r, 0, sizeof(r));
+    r.k = uint32_t(nterms);
+    r.nctrl = uint32_t(__builtin_popcountll(cm));
+    r.nqubits = N_;
+    r.bytes = uint64_t(nterms + 1) * (uint64_t(1) << N_) * 16;
+    r.precision = uint32_t(prec_);
+    r.kind = 4;
+    const double t_taylor = double(s) * double(K) * (predict_ms(r) + kOrderRoundTripMs);
+    r.kind = 5;
+    const double t_cheb = double(ncheb) * (predict_ms(r) + kStepGapMs);
+    last_te_pred_[0] = t_taylor;
+    last_te_pred_[1] = t_cheb;
+    return t_cheb < t_taylor;
   }
 
   // ---- simulator.hpp:352-368 ----------------------------------------------
@@ -775,7 +830,7 @@ class Engine {
   // The cost model maps the features of one kernel launch (launch_features)
   // to its predicted log(milliseconds); the learned planner sums predictions
   // over candidate plans of the queued gates.
-  static constexpr int kFeatures = 16;
+  static constexpr int kFeatures = 20;
   void set_cost_model(int F, int H, const float *params) {
     if (F != kFeatures || H < 1 || H > 256) fail(GSIM_ERR_VALUE, "cost model: unexpected layer sizes");
     cm_H_ = H;
@@ -1186,6 +1241,7 @@ class Engine {
   std::array<UploadSlot, 4> mslots_;
   size_t mslot_next_ = 0;
   std::vector<float> cm_;  // cost-model weights (host copy)
+  double last_te_pred_[2] = {0., 0.};  // predicted ms of the series and the expansion, last evolution
   int cm_H_ = 0;
   int last_choice_ = -1;
   std::vector<uint8_t> learned_ok_ = std::vector<uint8_t>(65, 1);
@@ -1421,7 +1477,7 @@ void Engine::exec_stage(const StagePlan &sp, const void *d_ops, const void *d_po
     p.rec.bytes = bytes;
     p.rec.precision = uint32_t(prec_);
     p.rec.ngates = sp.ngates;
-    p.rec.aux = uint32_t(sp.subs.size());
+    p.rec.aux = sp.pk.empty() ? uint32_t(sp.subs.size()) : (sp.pk_nsubs | (1u << 16));
     p.ev0 = e0;
     p.ev1 = e1;
     prof_.push_back(p);
@@ -1515,13 +1571,20 @@ void launch_features(const gsim_launch_record &r, float *f) {
   auto lg = [](double x) { return float(std::log2(1.0 + x)); };
   f[0] = float(r.nqubits) / 32.f;
   f[1] = r.precision == GSIM_C64 ? 1.f : 0.f;
-  f[2 + std::min<uint32_t>(r.kind, 3u)] = 1.f;
   double flops;
-  if (r.kind == 1) {  // stage: k = operations, aux = register substages (0: one pass per operation)
+  if (r.kind == 4 || r.kind == 5) {  // a Taylor-series or Chebyshev step of emulate_time_evolution: k = terms
+    f[r.kind == 4 ? 17 : 18] = 1.f;
+    f[19] = float(r.k) / 64.f;
+    f[7] = float(r.nctrl) / 8.f;
+    flops = amps * double(r.k);
+  } else if (r.kind == 1) {  // stage: k = operations, aux = substages | packed-pair flag << 16
+    f[3] = 1.f;
     flops = amps * double(r.k);
     f[12] = float(r.k) / 64.f;
-    f[13] = float(r.aux) / 32.f;
+    f[13] = float(r.aux & 0xFFFFu) / 32.f;
+    f[16] = (r.aux >> 16) & 1u ? 1.f : 0.f;
   } else {
+    f[2 + std::min<uint32_t>(r.kind, 3u)] = 1.f;
     const double touched = std::ldexp(1.0, int(r.nqubits) - int(r.nctrl));
     flops = touched * std::ldexp(1.0, int(r.k));
     f[6] = float(r.k) / 8.f;
@@ -1588,10 +1651,10 @@ double Engine::predict_ms(const gsim_launch_record &r) {
   // The features depend only on these fields (bytes follows from nqubits,
   // nctrl and precision), so they key the memo of predictions.
   const uint64_t lowt = r.targets ? uint64_t(__builtin_ctzll(r.targets)) : 0;
-  const uint64_t key = uint64_t(r.kind & 3u) | (uint64_t(r.k & 255u) << 2) | (uint64_t(r.nctrl & 63u) << 10) |
-                       (lowt << 16) | (uint64_t(__builtin_popcountll(r.targets & 0xFull)) << 22) |
-                       (uint64_t(r.nqubits & 63u) << 25) | (uint64_t(r.precision & 1u) << 31) |
-                       (uint64_t(r.aux & 0xFFFFu) << 32);
+  const uint64_t key = uint64_t(r.kind & 7u) | (uint64_t(r.k & 255u) << 3) | (uint64_t(r.nctrl & 63u) << 11) |
+                       (lowt << 17) | (uint64_t(__builtin_popcountll(r.targets & 0xFull)) << 23) |
+                       (uint64_t(r.nqubits & 63u) << 26) | (uint64_t(r.precision & 1u) << 32) |
+                       (uint64_t(r.aux & 0x1FFFFu) << 33);
   auto it = memo_.find(key);
   if (it != memo_.end()) return it->second;
   float f[kFeatures];
@@ -1620,7 +1683,7 @@ double Engine::staged_ms(const std::vector<PlanStep> &steps) {
     std::memset(&r, 0, sizeof(r));
     r.kind = 1;
     r.k = uint32_t(st.stage.ops.size());
-    r.aux = uint32_t(st.stage.subs.size());
+    r.aux = st.stage.pk.empty() ? uint32_t(st.stage.subs.size()) : (st.stage.pk_nsubs | (1u << 16));
     r.nqubits = N_;
     r.bytes = 2 * (uint64_t(1) << N_) * bpa_;
     r.precision = uint32_t(prec_);
@@ -2131,7 +2194,7 @@ int gsim_compare_states(gsim_engine *a, gsim_engine *b, double *out) {
 }
 int gsim_launch_features(const gsim_launch_record *recs, size_t n, float *out, size_t nfeat) {
   return guard([&] {
-    if (nfeat < size_t(Engine::kFeatures)) fail(GSIM_ERR_LENGTH, "launch_features(): nfeat < 16");
+    if (nfeat < size_t(Engine::kFeatures)) fail(GSIM_ERR_LENGTH, "launch_features(): nfeat < 20");
     for (size_t i = 0; i < n; ++i) {
       float f[Engine::kFeatures];
       gsim::launch_features(recs[i], f);

@@ -500,7 +500,9 @@ __device__ __forceinline__ void dense1(f2 (&RE)[16], f2 (&IM)[16], const f2 *__r
   X00 = M[0]; X01 = M[1]; X10 = M[2]; X11 = M[3];
   if constexpr (CLS != 1) {
     Y00 = M[4]; Y01 = M[5]; Y10 = M[6]; Y11 = M[7];
-    N00 = M[8]; N01 = M[9]; N10 = M[10]; N11 = M[11];
+    // -Y as negated operands (free in the packed FMA): fewer live registers
+    N00 = make_float2(-Y00.x, -Y00.y); N01 = make_float2(-Y01.x, -Y01.y);
+    N10 = make_float2(-Y10.x, -Y10.y); N11 = make_float2(-Y11.x, -Y11.y);
   }
 #pragma unroll
   for (int j = 0; j < 16; ++j) {

@@ -14,31 +14,31 @@ gates per pass.  Allocating a qubit, U -> I2 (x) U (_unitary.py:197-201),
 adds a row and a column qubit in |0> and maps that pair |00> -> |00> + |11>
 with one exact 0/1 two-qubit matrix.
 
-Everything else follows the reference class: the qubit map and its shift on
-deallocation, validity and the reset into ``history`` (with the same
-warning) on the first gate after a measurement or deallocation, the host
-state vector updated as ``unitary @ state`` on flush, and measurement with
-Python's ``random`` on that state (_unitary.py:248-285).
+The class derives from ProjectQ's own UnitarySimulator and leaves it the
+parts that do not touch the unitary's storage: command dispatch
+(``receive``), availability, deallocation (the qubit-map shift), the
+measurement command (its checks and LogicalQubitIDTag handling) and
+``history``.  It replaces allocation, the gate branch (including the reset
+into ``history`` on the first gate after a measurement or deallocation), the
+flush (host state <- U @ state) and the sampling of a measurement, which is
+vectorised here and picks the same outcome as the reference's loop for the
+same ``random.random()`` draw (_unitary.py:248-285).
 """
 
 from __future__ import annotations
 
-import math
 import random
 import warnings
-from copy import deepcopy
 
 import numpy as np
 
 from .simulator import Simulator
 
-try:  # ProjectQ's engine base class; the class is only usable with ProjectQ installed
-    from projectq.cengines import BasicEngine
-    from projectq.meta import LogicalQubitIDTag, get_control_count, has_negative_control
+try:  # ProjectQ's own class is the base; this module is only usable with ProjectQ installed
+    from projectq.backends._unitary import UnitarySimulator as _ProjectQUnitarySimulator
     from projectq.ops import AllocateQubitGate, DeallocateQubitGate, FlushGate, MeasureGate
-    from projectq.types import WeakQubitRef
 except ImportError:  # pragma: no cover - exercised only without ProjectQ
-    BasicEngine = object
+    _ProjectQUnitarySimulator = object
     _PROJECTQ = False
 else:
     _PROJECTQ = True
@@ -93,136 +93,92 @@ class _DeviceUnitary:
         self.sim.close()
 
 
-class UnitarySimulator(BasicEngine):
+class UnitarySimulator(_ProjectQUnitarySimulator):
     """Drop-in for projectq.backends.UnitarySimulator with the unitary on the GPU.
 
     Extra keyword: ``precision`` ("c128", the reference's complex, or "c64").
     """
 
+    _RESET_WARNING = ("Processing of other gates after a qubit deallocation or measurement will reset the unitary,"
+                      "previous unitary can be accessed in history")
+
     def __init__(self, precision="c128", _api=None):
         if not _PROJECTQ:
-            raise ImportError("UnitarySimulator needs ProjectQ (projectq.cengines.BasicEngine)")
+            raise ImportError("UnitarySimulator needs ProjectQ (projectq.backends.UnitarySimulator)")
         super().__init__()
         self._precision = precision
         self._api = _api
-        self._qubit_map = {}
         self._dev = _DeviceUnitary(0, precision, _api)
-        self._num_qubits = 0
-        self._is_valid = True
-        self._is_flushed = False
-        self._state = [1]
-        self._history = []
+        self._state = np.ones(1, dtype=np.complex128)
 
     @property
     def unitary(self):
-        """The current unitary (a copy), as _unitary.py:102-110."""
+        """The current unitary, downloaded from the device as a NumPy matrix."""
         return self._dev.matrix()
 
-    @property
-    def history(self):
-        """Previous unitaries, one per reset after a measurement or deallocation."""
-        return deepcopy(self._history)
-
-    def is_available(self, cmd):
-        """_unitary.py:124-149: arbitrarily controlled gates with a matrix."""
-        if has_negative_control(cmd):
-            return False
-        if isinstance(cmd.gate, (AllocateQubitGate, DeallocateQubitGate, MeasureGate)):
-            return True
-        try:
-            gate_mat = cmd.gate.matrix
-            if len(gate_mat) > 2**6:
-                warnings.warn(f"Potentially large matrix gate encountered! ({math.log2(len(gate_mat))} qubits)")
-            return True
-        except AttributeError:
-            return False
-
-    def receive(self, command_list):
-        for cmd in command_list:
-            self._handle(cmd)
-        if not self.is_last_engine:
-            self.send(command_list)
-
     def _flush(self):
-        """_unitary.py:170-174: state <- unitary @ state, once per flush."""
-        if not self._is_flushed:
-            self._is_flushed = True
-            self._state = self.unitary @ np.asarray(self._state, dtype=np.complex128)
+        if self._is_flushed:
+            return
+        self._is_flushed = True
+        self._state = self._dev.matrix() @ np.asarray(self._state, dtype=np.complex128)
 
     def _handle(self, cmd):
-        """_unitary.py:176-246."""
-        if isinstance(cmd.gate, AllocateQubitGate):
-            self._qubit_map[cmd.qubits[0][0].id] = self._num_qubits
-            self._num_qubits += 1
-            self._dev.add_qubit()
-            self._state = list(self._state) + [0] * len(self._state)
-
-        elif isinstance(cmd.gate, DeallocateQubitGate):
-            pos = self._qubit_map[cmd.qubits[0][0].id]
-            self._qubit_map = {key: value - 1 if value > pos else value for key, value in self._qubit_map.items()}
-            self._num_qubits -= 1
-            self._is_valid = False
-
-        elif isinstance(cmd.gate, MeasureGate):
-            self._is_valid = False
-            if not self._is_flushed:
-                raise RuntimeError(
-                    'Please make sure all previous gates are flushed before measurement so the state gets updated'
-                )
-            if get_control_count(cmd) != 0:
-                raise ValueError('Cannot have control qubits with a measurement gate!')
-            all_qubits = [qb for qr in cmd.qubits for qb in qr]
-            measurements = self.measure_qubits([qb.id for qb in all_qubits])
-            for qb, res in zip(all_qubits, measurements):
-                for tag in cmd.tags:
-                    if isinstance(tag, LogicalQubitIDTag):
-                        qb = WeakQubitRef(qb.engine, tag.logical_qubit_id)
-                        break
-                self.main_engine.set_measurement_result(qb, res)
-
-        elif isinstance(cmd.gate, FlushGate):
-            self._flush()
+        gate = cmd.gate
+        if isinstance(gate, AllocateQubitGate):
+            self._allocate(cmd.qubits[0][0].id)
+        elif isinstance(gate, (DeallocateQubitGate, MeasureGate, FlushGate)):
+            super()._handle(cmd)  # the base class: map shift, measurement checks and tags, flush dispatch
         else:
-            if not self._is_valid:
-                self._flush()
-                warnings.warn(
-                    "Processing of other gates after a qubit deallocation or measurement will reset the unitary,"
-                    "previous unitary can be accessed in history"
-                )
-                self._history.append(self.unitary)
-                self._dev.close()
-                self._dev = _DeviceUnitary(self._num_qubits, self._precision, self._api)
-                self._state = np.array([1] + ([0] * (2**self._num_qubits - 1)), dtype=complex)
-                self._is_valid = True
-            self._is_flushed = False
-            targets = [self._qubit_map[qb.id] for qr in cmd.qubits for qb in qr]
-            controls = [self._qubit_map[qb.id] for qb in cmd.control_qubits]
-            self._dev.apply(np.asarray(cmd.gate.matrix, dtype=np.complex128), targets, controls)
+            self._apply(cmd)
+
+    def _allocate(self, qubit_id):
+        # the newest qubit is the most significant bit of the unitary and state
+        self._qubit_map[qubit_id] = self._num_qubits
+        self._num_qubits += 1
+        self._dev.add_qubit()
+        state = np.asarray(self._state, dtype=np.complex128)
+        self._state = np.concatenate([state, np.zeros_like(state)])
+
+    def _restart(self):
+        """After a measurement or deallocation: the unitary so far goes to
+        history and a fresh identity starts on the current qubits, from |0...0>."""
+        self._flush()
+        warnings.warn(self._RESET_WARNING)
+        self._history.append(self._dev.matrix())
+        self._dev.close()
+        self._dev = _DeviceUnitary(self._num_qubits, self._precision, self._api)
+        self._state = np.zeros(1 << self._num_qubits, dtype=np.complex128)
+        self._state[0] = 1.0
+        self._is_valid = True
+
+    def _apply(self, cmd):
+        if not self._is_valid:
+            self._restart()
+        self._is_flushed = False
+        pos = self._qubit_map
+        self._dev.apply(np.asarray(cmd.gate.matrix, dtype=np.complex128),
+                        [pos[qb.id] for qr in cmd.qubits for qb in qr], [pos[qb.id] for qb in cmd.control_qubits])
 
     def measure_qubits(self, ids):
-        """_unitary.py:248-285: sample from the flushed host state, project, renormalise."""
-        random_outcome = random.random()
-        state = np.asarray(self._state, dtype=np.complex128)
-        val = 0.0
-        i_picked = 0
-        while val < random_outcome and i_picked < len(state):
-            val += np.abs(state[i_picked]) ** 2
-            i_picked += 1
-        i_picked -= 1
-        pos = [self._qubit_map[ID] for ID in ids]
-        res = [False] * len(pos)
-        mask = 0
-        val = 0
-        for i, _pos in enumerate(pos):
-            res[i] = ((i_picked >> _pos) & 1) == 1
-            mask |= 1 << _pos
-            val |= (res[i] & 1) << _pos
-        nrm = 0.0
-        for i, amp in enumerate(state):
-            if (mask & i) != val:
-                state[i] = 0.0
-            else:
-                nrm += np.abs(amp) ** 2
-        state *= 1.0 / np.sqrt(nrm)
+        """Sample basis state i with probability |state_i|^2 (the draw is one
+        random.random(); the running sum is NumPy's sequential cumsum, so the
+        outcome equals the reference's element loop, including its draw of
+        exactly 0.0 selecting index -1), then project and renormalise."""
+        draw = random.random()
+        state = np.array(self._state, dtype=np.complex128)
+        probs = np.abs(state) ** 2
+        running = np.cumsum(probs)
+        if draw <= 0.0:
+            pick = -1
+        else:
+            pick = min(int(np.searchsorted(running, draw, side="left")), state.size - 1)
+        positions = [self._qubit_map[q] for q in ids]
+        outcome = [bool((pick >> p) & 1) for p in positions]
+        mask = sum(1 << p for p in positions)
+        value = sum(int(o) << p for o, p in zip(outcome, positions))
+        keep = (np.arange(state.size, dtype=np.int64) & mask) == value
+        norm = np.cumsum(np.where(keep, probs, 0.0))[-1]
+        state[~keep] = 0.0
+        state *= 1.0 / np.sqrt(norm)
         self._state = state
-        return res
+        return outcome
