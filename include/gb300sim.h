@@ -332,7 +332,8 @@ GSIM_API int gsim_adjoint_gradient(gsim_engine *e, size_t nops, const uint8_t *k
  * nfeat >= 20), the same function the planner applies to candidate launches;
  * needs no engine and no GPU.
  * gsim_set_cost_model: install trained weights (nfeatures = 20, `hidden`
- * units per layer, layout of gsim_mlp_get_params).
+ * units per layer, layout of gsim_mlp_get_params; params must hold all
+ * H*F + H + H*H + H + H + 1 values, it is read without a length).
  * gsim_set_learned_regimes: allowed[n] != 0 lets learned plans run on
  * n-qubit states (n < count <= 65); elsewhere, and without a cost model, the
  * learned mode runs the greedy fixed-size fusion.

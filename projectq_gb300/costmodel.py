@@ -258,7 +258,11 @@ def install(sim, params=None, regimes=None):
         params = shipped["params"] if params is None else params
         if regimes is None:
             regimes = shipped["regimes_" + sim.precision]
-    p = np.ascontiguousarray(params, dtype=np.float32)
+    p = np.ascontiguousarray(params, dtype=np.float32).reshape(-1)
+    want = H * F + H + H * H + H + H + 1
+    if p.size != want:
+        raise ValueError(f"cost model: {p.size} parameters, the {F} -> {H} -> {H} -> 1 network has {want} "
+                         "(weights of another feature set: retrain with python -m projectq_gb300.costmodel)")
     _lib.check(sim._api, sim._api.set_cost_model(sim._h, F, H, _fp(p)))
     if regimes is not False:
         r = np.ascontiguousarray(regimes, dtype=np.uint8)

@@ -481,16 +481,37 @@ __global__ void __launch_bounds__(256, R > 4 ? 2 : 3) stage_reg_kernel(cplx_t<T>
 // stage's pack bit, which no operation touches.  Every operation therefore
 // treats both halves alike and runs on packed f32x2 FMAs (one instruction per
 // two amplitudes).  Shared memory holds the tile as two arrays of pairs,
-// tre / tim[s(q)]; descriptors, offset tables, matrices (entries as broadcast
+// one 16-byte element per pair, tp[s(q)] = (RE, IM); descriptors, offset tables, matrices (entries as broadcast
 // pairs (x, x), (y, y), (-y, -y)) and diagonal tables live in shared memory
 // too and are read with warp-broadcast 16-byte loads.
 namespace pk {
 
-using f2 = float2;
-__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) { return __ffma2_rn(a, b, c); }
-__device__ __forceinline__ f2 mul2(f2 a, f2 b) { return __fmul2_rn(a, b); }
+// A pair of floats lives in one 64-bit register pair (low half = the
+// amplitude with pack bit 0), and the packed FMAs take it as one .b64
+// operand: with float2 (two separate 32-bit values) the compiler re-paired
+// the halves around every packed instruction (two integer-pipe moves per
+// 64-bit value per operation, measured).
+using f2 = unsigned long long;
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 neg2(f2 a) { return a ^ 0x8000000080000000ull; }  // both halves' signs
+__device__ __forceinline__ f2 pack2(float lo, float hi) {
+  f2 d;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(d) : "f"(lo), "f"(hi));
+  return d;
+}
+__device__ __forceinline__ float lo2(f2 a) { return __uint_as_float(uint32_t(a)); }
+__device__ __forceinline__ float hi2(f2 a) { return __uint_as_float(uint32_t(a >> 32)); }
 
-__device__ __forceinline__ uint32_t swz(uint32_t q) { return q ^ (((q >> 4) ^ (q >> 8)) & 15u); }
+__device__ __forceinline__ uint32_t swz(uint32_t q) { return q ^ (((q >> 3) ^ (q >> 6) ^ (q >> 9)) & 7u); }
 
 // Dense 1-qubit operation on register pair-bit B; M = X00 X01 X10 X11,
 // Y00 Y01 Y10 Y11, N00 N01 N10 N11 (N = -Y), each a broadcast pair.
@@ -501,8 +522,7 @@ __device__ __forceinline__ void dense1(f2 (&RE)[16], f2 (&IM)[16], const f2 *__r
   if constexpr (CLS != 1) {
     Y00 = M[4]; Y01 = M[5]; Y10 = M[6]; Y11 = M[7];
     // -Y as negated operands (free in the packed FMA): fewer live registers
-    N00 = make_float2(-Y00.x, -Y00.y); N01 = make_float2(-Y01.x, -Y01.y);
-    N10 = make_float2(-Y10.x, -Y10.y); N11 = make_float2(-Y11.x, -Y11.y);
+    N00 = neg2(Y00); N01 = neg2(Y01); N10 = neg2(Y10); N11 = neg2(Y11);
   }
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
@@ -573,10 +593,10 @@ __device__ __forceinline__ void cmul(f2 &re, f2 &im, f2 fx, f2 fy, f2 fn) {
 }
 
 template <int B>
-__device__ __forceinline__ void diag1(f2 (&RE)[16], f2 (&IM)[16], const float4 *e0, const float4 *e1) {
-  const float4 a0 = e0[0], b0 = e0[1], a1 = e1[0], b1 = e1[1];
-  const f2 x0 = make_float2(a0.x, a0.y), y0 = make_float2(a0.z, a0.w), n0 = make_float2(b0.x, b0.y);
-  const f2 x1 = make_float2(a1.x, a1.y), y1 = make_float2(a1.z, a1.w), n1 = make_float2(b1.x, b1.y);
+__device__ __forceinline__ void diag1(f2 (&RE)[16], f2 (&IM)[16], const ulonglong2 *e0, const ulonglong2 *e1) {
+  const ulonglong2 a0 = e0[0], b0 = e0[1], a1 = e1[0], b1 = e1[1];
+  const f2 x0 = a0.x, y0 = a0.y, n0 = b0.x;
+  const f2 x1 = a1.x, y1 = a1.y, n1 = b1.x;
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     if ((j >> B) & 1) cmul(RE[j], IM[j], x1, y1, n1);
@@ -632,16 +652,16 @@ __device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsig
     const uint32_t bit = (sidx & 0x80u) ? uint32_t((base >> (sidx & 0x7Fu)) & 1u) : (row >> sidx) & 1u;
     cidx |= bit << op.sbit[i];
   }
-  const float4 *T = reinterpret_cast<const float4 *>(blob + op.data);  // 32-byte entries
+  const ulonglong2 *T = reinterpret_cast<const ulonglong2 *>(blob + op.data);  // 32-byte entries
   if (kind == kPkDiag0) {
-    const float4 a = T[2 * cidx], b = T[2 * cidx + 1];
-    const f2 x = make_float2(a.x, a.y), y = make_float2(a.z, a.w), n = make_float2(b.x, b.y);
+    const ulonglong2 a = T[2 * cidx], b = T[2 * cidx + 1];
+    const f2 x = a.x, y = a.y, n = b.x;
 #pragma unroll
     for (int j = 0; j < 16; ++j) cmul(RE[j], IM[j], x, y, n);
     return;
   }
   if (kind == kPkDiag1) {
-    const float4 *e0 = T + 2 * cidx, *e1 = T + 2 * (cidx | (1u << op.dq));
+    const ulonglong2 *e0 = T + 2 * cidx, *e1 = T + 2 * (cidx | (1u << op.dq));
     switch (B) {
       case 0: diag1<0>(RE, IM, e0, e1); break;
       case 1: diag1<1>(RE, IM, e0, e1); break;
@@ -656,8 +676,8 @@ __device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsig
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     const uint32_t idx = cidx | ((jw[j >> 2] >> (8 * (j & 3))) & 0xFFu);
-    const float4 a = T[2 * idx], b = T[2 * idx + 1];
-    cmul(RE[j], IM[j], make_float2(a.x, a.y), make_float2(a.z, a.w), make_float2(b.x, b.y));
+    const ulonglong2 a = T[2 * idx], b = T[2 * idx + 1];
+    cmul(RE[j], IM[j], a.x, a.y, b.x);
   }
 }
 
@@ -668,8 +688,7 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
                                                           uint32_t blob_bytes, uint32_t nsubs, uint32_t P) {
   using pk::f2;
   extern __shared__ __align__(16) unsigned char smem[];
-  f2 *tre = reinterpret_cast<f2 *>(smem);
-  f2 *tim = tre + 4096;
+  ulonglong2 *tp = reinterpret_cast<ulonglong2 *>(smem);  // tp[s(q)] = (RE, IM) of pair q
   uint64_t *segoff = reinterpret_cast<uint64_t *>(smem + 65536);
   const uint32_t nseg = 1u << A.h;
   unsigned char *blob = smem + 65536 + ((nseg * 8 + 15) & ~15u);
@@ -686,8 +705,13 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
   const PkOpDev *ops = reinterpret_cast<const PkOpDev *>(blob + ((nsubs * sizeof(PkSubDev) + 15) & ~15u));
   const uint32_t row = threadIdx.x;
   const uint32_t rmask = (1u << A.m) - 1;
-  for (uint64_t t = blockIdx.x; t < A.ntiles; t += gridDim.x) {
-    const uint64_t base = insert_zeros(t, A.lpos, int(A.L));
+  // The first tile is loaded here; each later tile's loads are issued in the
+  // same loop that writes the previous tile back (every shared-memory slot
+  // is read, written to HBM and refilled by one thread), so their latency
+  // overlaps the stores and one barrier per tile goes.
+  uint64_t t = blockIdx.x;
+  uint64_t base = t < A.ntiles ? insert_zeros(t, A.lpos, int(A.L)) : 0;
+  if (t < A.ntiles) {
     // HBM -> shared memory: pairs along P (tile position p = q with bit P inserted)
     if (P == 0) {
       float4 x[16];
@@ -699,8 +723,7 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
 #pragma unroll
       for (int i = 0; i < 16; ++i) {
         const uint32_t sq = pk::swz(threadIdx.x + 256u * i);
-        tre[sq] = make_float2(x[i].x, x[i].z);
-        tim[sq] = make_float2(x[i].y, x[i].w);
+        tp[sq] = make_ulonglong2(pk::pack2(x[i].x, x[i].z), pk::pack2(x[i].y, x[i].w));
       }
     } else {
       float4 x[8], y[8];
@@ -715,13 +738,13 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
       for (int i = 0; i < 8; ++i) {
         const uint32_t q = (threadIdx.x + 256u * i) << 1;
         const uint32_t s0 = pk::swz(q), s1 = pk::swz(q + 1);
-        tre[s0] = make_float2(x[i].x, y[i].x);
-        tim[s0] = make_float2(x[i].y, y[i].y);
-        tre[s1] = make_float2(x[i].z, y[i].z);
-        tim[s1] = make_float2(x[i].w, y[i].w);
+        tp[s0] = make_ulonglong2(pk::pack2(x[i].x, y[i].x), pk::pack2(x[i].y, y[i].y));
+        tp[s1] = make_ulonglong2(pk::pack2(x[i].z, y[i].z), pk::pack2(x[i].w, y[i].w));
       }
     }
-    __syncthreads();
+  }
+  __syncthreads();
+  while (t < A.ntiles) {
     for (uint32_t si = 0; si < nsubs; ++si) {
       const PkSubDev S = subs[si];
       const uint32_t *tab = reinterpret_cast<const uint32_t *>(blob + S.tab);
@@ -744,8 +767,9 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const uint32_t a = a0 ^ off[e];
-            RE[4 * g + e] = tre[a];
-            IM[4 * g + e] = tim[a];
+            const ulonglong2 v = tp[a];
+            RE[4 * g + e] = v.x;
+            IM[4 * g + e] = v.y;
           }
         }
       }
@@ -771,34 +795,70 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const uint32_t a = a0 ^ off[e];
-            tre[a] = RE[4 * g + e];
-            tim[a] = IM[4 * g + e];
+            tp[a] = make_ulonglong2(RE[4 * g + e], IM[4 * g + e]);
           }
         }
       }
       __syncthreads();
     }
-    // shared memory -> HBM
+    // shared memory -> HBM, and the next tile's loads into the same slots
+    const uint64_t tn = t + gridDim.x;
+    const bool more = tn < A.ntiles;
+    // past the last tile the loads re-read the current tile (valid addresses,
+    // the data is never used): no conditional around them
+    const uint64_t bn = more ? insert_zeros(tn, A.lpos, int(A.L)) : base;
     if (P == 0) {
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {  // two halves: 8 loads in flight per thread, fewer live registers
+        asm volatile("" ::: "memory");  // keep the second half's loads after the first half's stores
+        float4 x[8];
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const uint32_t q = threadIdx.x + 256u * i, p = q << 1;
-        const uint32_t sq = pk::swz(q);
-        const f2 r = tre[sq], m = tim[sq];
-        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & rmask)), make_float4(r.x, m.x, r.y, m.y));
+        for (int i = 0; i < 8; ++i) {
+          const uint32_t p = (threadIdx.x + 256u * (i + 8 * h)) << 1;
+          x[i] = __ldcs(reinterpret_cast<const float4 *>(psi + bn + segoff[p >> A.m] + (p & rmask)));
+        }
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const uint32_t q = threadIdx.x + 256u * (i + 8 * h), p = q << 1;
+          const uint32_t sq = pk::swz(q);
+          const ulonglong2 v = tp[sq];
+          const f2 r = v.x, m = v.y;
+          __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p >> A.m] + (p & rmask)),
+                 make_float4(pk::lo2(r), pk::lo2(m), pk::hi2(r), pk::hi2(m)));
+          tp[sq] = make_ulonglong2(pk::pack2(x[i].x, x[i].z), pk::pack2(x[i].y, x[i].w));
+        }
       }
     } else {
+#pragma unroll 1
+      for (int h = 0; h < 2; ++h) {
+        asm volatile("" ::: "memory");
+        float4 x[4], y[4];
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        const uint32_t q = (threadIdx.x + 256u * i) << 1;
-        const uint32_t p0 = ((q >> P) << (P + 1)) | (q & ((1u << P) - 1)), p1 = p0 | (1u << P);
-        const uint32_t s0 = pk::swz(q), s1 = pk::swz(q + 1);
-        const f2 r0 = tre[s0], m0 = tim[s0], r1 = tre[s1], m1 = tim[s1];
-        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p0 >> A.m] + (p0 & rmask)), make_float4(r0.x, m0.x, r1.x, m1.x));
-        __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p1 >> A.m] + (p1 & rmask)), make_float4(r0.y, m0.y, r1.y, m1.y));
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t q = (threadIdx.x + 256u * (i + 4 * h)) << 1;
+          const uint32_t p0 = ((q >> P) << (P + 1)) | (q & ((1u << P) - 1)), p1 = p0 | (1u << P);
+          x[i] = __ldcs(reinterpret_cast<const float4 *>(psi + bn + segoff[p0 >> A.m] + (p0 & rmask)));
+          y[i] = __ldcs(reinterpret_cast<const float4 *>(psi + bn + segoff[p1 >> A.m] + (p1 & rmask)));
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t q = (threadIdx.x + 256u * (i + 4 * h)) << 1;
+          const uint32_t p0 = ((q >> P) << (P + 1)) | (q & ((1u << P) - 1)), p1 = p0 | (1u << P);
+          const uint32_t s0 = pk::swz(q), s1 = pk::swz(q + 1);
+          const ulonglong2 v0 = tp[s0], v1 = tp[s1];
+          const f2 r0 = v0.x, m0 = v0.y, r1 = v1.x, m1 = v1.y;
+          __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p0 >> A.m] + (p0 & rmask)),
+                 make_float4(pk::lo2(r0), pk::lo2(m0), pk::lo2(r1), pk::lo2(m1)));
+          __stcs(reinterpret_cast<float4 *>(psi + base + segoff[p1 >> A.m] + (p1 & rmask)),
+                 make_float4(pk::hi2(r0), pk::hi2(m0), pk::hi2(r1), pk::hi2(m1)));
+          tp[s0] = make_ulonglong2(pk::pack2(x[i].x, y[i].x), pk::pack2(x[i].y, y[i].y));
+          tp[s1] = make_ulonglong2(pk::pack2(x[i].z, y[i].z), pk::pack2(x[i].w, y[i].w));
+        }
       }
     }
     __syncthreads();
+    t = tn;
+    base = bn;
   }
 }
 

@@ -357,14 +357,15 @@ inline void build_substages(StagePlan &sp, unsigned r, unsigned rho) {
 // The packed-pair stage kernel (kernels_stage.cu, stage_pk_kernel) needs a
 // tile bit P that no operation of the stage touches.  Amplitudes are held as
 // pairs along P: a "pair" q is a tile position with bit P removed (12 bits),
-// and shared memory keeps two arrays of float2, re[q] = (Re psi(q, P=0),
-// Re psi(q, P=1)) and im[q] likewise.  Every operation acts on both halves of
+// and shared memory keeps one 16-byte element per pair, (Re psi(q, P=0),
+// Re psi(q, P=1), Im psi(q, P=0), Im psi(q, P=1)).  Every operation acts on both halves of
 // a pair identically (P is not among its qubits), so the arithmetic runs on
 // packed f32x2 FMAs.  A thread holds 16 pairs (32 amplitudes): register index
 // jj over 4 register pair-bits, and its row (0..255) over the other 8.
-// Pair positions in shared memory are swizzled, s(q) = q ^ fold4(q >> 4), so
-// pair-bit b lands in bank class b mod 4; a substage's lanes cover all four
-// classes where its register choice leaves them free.
+// Pair positions in shared memory are swizzled, s(q) = q ^ fold3(q >> 3), so
+// pair-bit b lands in bank class b mod 3; a substage's first three lanes
+// cover the three classes where its register choice leaves them free, which
+// makes the 16-byte accesses of each quarter warp conflict-free.
 constexpr unsigned kPkTileBits = 13;      // 2^13 amplitudes = 4096 pairs per tile
 constexpr size_t kPkBlobMax = 40 * 1024;  // shared-memory budget for descriptors, tables and data
 
@@ -401,7 +402,7 @@ struct alignas(16) PkOpDev {
 };
 static_assert(sizeof(PkOpDev) == 64, "PkOpDev is read with 16-byte loads");
 
-inline uint32_t pk_swizzle(uint32_t q) { return tile_swizzle(q, 4); }
+inline uint32_t pk_swizzle(uint32_t q) { return tile_swizzle(q, 3); }
 
 // Build the packed-pair substages of a complex64 stage whose plan has a pack
 // bit (sp.pack >= 0, untouched by every operation) and only 1-qubit dense
@@ -468,14 +469,14 @@ inline bool build_substages_pk(StagePlan &sp) {
         progress = true;
       }
     }
-    // pad to 5 register bits, from the bank classes (pair-bit mod 4) with most spare bits
+    // pad to 5 register bits, from the bank classes (pair-bit mod 3) with most spare bits
     while (unsigned(__builtin_popcount(R)) < 5) {
       int best = -1, best_count = -1;
       for (unsigned b = 0; b < L; ++b) {
         if ((R >> b) & 1) continue;
         int cnt = 0;
         for (unsigned c = 0; c < L; ++c)
-          if (!((R >> c) & 1) && c != P && qbit(c) % 4 == qbit(b) % 4) ++cnt;
+          if (!((R >> c) & 1) && c != P && qbit(c) % 3 == qbit(b) % 3) ++cnt;
         if (cnt > best_count) {
           best_count = cnt;
           best = int(b);
@@ -531,12 +532,12 @@ inline bool build_substages_pk(StagePlan &sp) {
         rq.push_back(qbit(b));
         rtile.push_back(b);
       }
-    std::vector<char> cls(4, 0);
+    std::vector<char> cls(3, 0);
     for (unsigned b = 0; b < L; ++b) {
       if (((R >> b) & 1)) continue;
       const unsigned qb = qbit(b);
-      if (!cls[qb % 4] && rows.size() < 4) {
-        cls[qb % 4] = 1;
+      if (!cls[qb % 3] && rows.size() < 3) {
+        cls[qb % 3] = 1;
         rows.push_back(qb);
       } else {
         rest.push_back(qb);

@@ -113,7 +113,8 @@ def test_learned_planner_applies_the_same_gates():
 def test_recorded_launches_carry_the_planner_features():
     """Profiling records of each planner map to features of the right kernel
     kind: greedy clusters of width k are dense launches with f[6] = k/8,
-    stages are kind 1 with their operation and substage counts."""
+    stages are kind 1 with their operation and substage counts and the
+    packed-pair flag."""
     n = 20
     gates = cm.random_circuit(np.random.default_rng(3), n, 20)
     recs = cm.record_launches(n, gates, "reference", 3)
@@ -124,7 +125,8 @@ def test_recorded_launches_carry_the_planner_features():
     recs = cm.record_launches(n, gates, "staged")
     f = cm.launch_features(recs)
     st = [(r, x) for r, x in zip(recs, f) if r["kind"] == 1]
-    assert st and all(x[12] == pytest.approx(r["k"] / 64) and x[13] == pytest.approx(r["aux"] / 32) for r, x in st)
+    assert st and all(x[12] == pytest.approx(r["k"] / 64) and x[13] == pytest.approx((r["aux"] & 0xFFFF) / 32)
+                      and x[16] == (1 if r["aux"] >> 16 else 0) for r, x in st)
 
 
 def test_without_a_model_learned_mode_runs_the_greedy_fusion():
