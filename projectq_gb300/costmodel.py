@@ -205,14 +205,15 @@ def record_evolution_launches(n, terms, t, mode, precision="c64"):
     return recs
 
 
-def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64", "c128"), te_every=3,
-            te_nmax=26):
+def collect(ncirc, seed=0, nmin=18, nmax=30, dmin=10, dmax=120, precisions=("c64", "c128"), te_every=3,
+            te_nmax=28, big=6):
     """Per-launch training set: features and log(ms) of every launch of
     `ncirc` random circuits, each run under every planner of COLLECT_PLANNERS;
     every `te_every`-th circuit also gives the step launches of a time
     evolution of a random 10-80-term Hamiltonian, by the series and by the
     expansion (short times: a step's cost does not depend on t, only the
-    number of steps does)."""
+    number of steps does); `big` more shallow complex64 circuits run on 31-32
+    qubits so that the largest states are inside the training range."""
     rng = np.random.default_rng(seed)
     feats, ys = [], []
 
@@ -221,12 +222,14 @@ def collect(ncirc, seed=0, nmin=18, nmax=28, dmin=10, dmax=120, precisions=("c64
             feats.append(launch_features(recs))
             ys.append(np.log(np.maximum(np.array([r["ms"] for r in recs], dtype=np.float64), 1e-4)))
 
-    for i in range(ncirc):
+    for i in range(ncirc + big):
         n = int(rng.integers(nmin, nmax + 1))
         prec = precisions[i % len(precisions)]
         if prec == "c128":
             n = min(n, nmax - 1)
         depth = int(rng.integers(dmin, dmax + 1))
+        if i >= ncirc:  # shallow circuits on the largest states, complex64
+            n, prec, depth = int(rng.integers(31, 33)), "c64", int(rng.integers(dmin, 21))
         gates = random_circuit(rng, n, depth)
         for fusion, kmax in COLLECT_PLANNERS[prec]:
             add(record_launches(n, gates, fusion, kmax, prec))
@@ -317,18 +320,21 @@ def wall_time(n, gates, fusion, precision="c64", params=None, regimes=None, tail
     return dt, choice
 
 
+TAIL_NMAX = 30  # the evolution's three complex128 vectors take 3 x 16 GiB at 30 qubits (192 GiB at 32)
+
+
 def _stream(rng, n, dmin, dmax, p_tail=0.1):
     depth = int(rng.integers(dmin, dmax + 1))
     gates = random_circuit(rng, n, depth)
     tail = None
-    if rng.uniform() < p_tail:
+    if rng.uniform() < p_tail and n <= TAIL_NMAX:
         ham = random_pauli_hamiltonian(n, nterms=50, seed=int(rng.integers(1 << 30)))
         terms = [(tuple(t), c) for t, c in ham if t]
         tail = (terms, float(rng.uniform(0, 1)))
     return gates, tail
 
 
-def calibrate(params, per_size=3, sizes=range(18, 31), precisions=("c64", "c128"), seed=7, dmin=10, dmax=120):
+def calibrate(params, per_size=3, sizes=range(18, 33), precisions=("c64", "c128"), seed=7, dmin=10, dmax=120):
     """The yardstick: per state size, total wall time of learned against greedy
     fixed-size fusion on `per_size` random circuits (not the training ones);
     returns {precision: uint8[65]} with 1 where learned was faster."""
@@ -337,7 +343,7 @@ def calibrate(params, per_size=3, sizes=range(18, 31), precisions=("c64", "c128"
     for prec in precisions:
         allowed = np.zeros(65, dtype=np.uint8)
         for n in sizes:
-            if prec == "c128" and n > max(sizes) - 1:
+            if prec == "c128" and n > 30:
                 continue
             tg = tl = 0.0
             for _ in range(per_size):
@@ -349,7 +355,7 @@ def calibrate(params, per_size=3, sizes=range(18, 31), precisions=("c64", "c128"
     return out
 
 
-def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=30, dmin=10, dmax=200, precision="c64",
+def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=32, dmin=10, dmax=200, precision="c64",
              with_staged=True, fidelity=True):
     """Config-5 style stream of `ncirc` random circuits (10% end with the time
     evolution of a 50-term Pauli Hamiltonian): wall time with the learned
