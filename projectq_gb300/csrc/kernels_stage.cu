@@ -604,6 +604,23 @@ __device__ __forceinline__ void diag1(f2 (&RE)[16], f2 (&IM)[16], const ulonglon
   }
 }
 
+// Diagonal whose register qubits are the register pair-bits in MASK: for
+// each value e of those bits, the table entry cidx | jidx[e] (jidx depends on
+// the masked bits only) multiplies every pair whose masked bits equal e.
+template <int MASK>
+__device__ __forceinline__ void diagm(f2 (&RE)[16], f2 (&IM)[16], const ulonglong2 *T, const uint8_t *jidx,
+                                      uint32_t cidx) {
+#pragma unroll
+  for (int e = 0; e < 16; ++e) {
+    if (e & ~MASK) continue;  // e runs over the values of the masked bits
+    const uint32_t idx = cidx | jidx[e];
+    const ulonglong2 a = T[2 * idx], b = T[2 * idx + 1];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if ((j & MASK) == e) cmul(RE[j], IM[j], a.x, a.y, b.x);
+  }
+}
+
 template <int B, int CLS>
 __device__ __forceinline__ void dense1_m(f2 (&RE)[16], f2 (&IM)[16], const f2 *M, uint32_t amask, bool masked) {
   if (masked) dense1<B, CLS, true>(RE, IM, M, amask);
@@ -670,14 +687,20 @@ __device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsig
     }
     return;
   }
-  // several register qubits: one table entry per register index
-  const uint4 jt = *reinterpret_cast<const uint4 *>(op.jidx);
-  const uint32_t jw[4] = {jt.x, jt.y, jt.z, jt.w};
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const uint32_t idx = cidx | ((jw[j >> 2] >> (8 * (j & 3))) & 0xFFu);
-    const ulonglong2 a = T[2 * idx], b = T[2 * idx + 1];
-    cmul(RE[j], IM[j], a.x, a.y, b.x);
+  // several register qubits, register-bit mask B (2 to 4 bits): one table
+  // entry per value of those bits, loaded once for all pairs sharing it
+  switch (B) {
+    case 3: diagm<3>(RE, IM, T, op.jidx, cidx); break;
+    case 5: diagm<5>(RE, IM, T, op.jidx, cidx); break;
+    case 6: diagm<6>(RE, IM, T, op.jidx, cidx); break;
+    case 9: diagm<9>(RE, IM, T, op.jidx, cidx); break;
+    case 10: diagm<10>(RE, IM, T, op.jidx, cidx); break;
+    case 12: diagm<12>(RE, IM, T, op.jidx, cidx); break;
+    case 7: diagm<7>(RE, IM, T, op.jidx, cidx); break;
+    case 11: diagm<11>(RE, IM, T, op.jidx, cidx); break;
+    case 13: diagm<13>(RE, IM, T, op.jidx, cidx); break;
+    case 14: diagm<14>(RE, IM, T, op.jidx, cidx); break;
+    default: diagm<15>(RE, IM, T, op.jidx, cidx); break;
   }
 }
 

@@ -382,13 +382,13 @@ enum : uint32_t {
   kPkSwap = 1,      // X on register pair-bit b (register controls in amask)
   kPkDiag0 = 2,     // diagonal without register qubits: one factor per thread
   kPkDiag1 = 3,     // diagonal with one register qubit (pair-bit b): two factors
-  kPkDiagN = 4,     // diagonal with several register qubits: a factor per register index
+  kPkDiagN = 4,     // diagonal with several register qubits (b: their pair-bit mask): a factor per value of them
   kPkLoadXor = 5,   // X folded into the load addresses (row / tile controls only)
   kPkStoreXor = 6,  // X folded into the store addresses
 };
 
 struct alignas(16) PkOpDev {
-  uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12
+  uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12 (kPkDiagN: b is a pair-bit mask)
   uint32_t data;     // blob offset of the operation's data (16-byte aligned)
   uint32_t amask;    // dense / swap with register controls: the register indices it pairs from (16 bits);
                      // folded X: the address XOR
@@ -620,7 +620,8 @@ inline bool build_substages_pk(StagePlan &sp) {
           }
         }
         cd.d.dq = dqb;
-        cd.d.code = (dreg == 0 ? kPkDiag0 : dreg == 1 ? kPkDiag1 : kPkDiagN) | (dbreg << 4);
+        // kPkDiag1: b = its register pair-bit; kPkDiagN: b = the mask of its register pair-bits
+        cd.d.code = dreg == 0 ? kPkDiag0 : dreg == 1 ? (kPkDiag1 | (dbreg << 4)) : (kPkDiagN | (cd.regs << 4));
       }
       cands.push_back(cd);
     }

@@ -249,7 +249,9 @@ void apply_stage_pk(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &
           const gsim::PkOpDev &op = ops[o];
           const uint32_t kind = op.code & 15u, B = (op.code >> 4) & 15u, cls = (op.code >> 8) & 15u;
           const bool masked = (op.code >> 12) & 1u;
-          if (kind == gsim::kPkLoadXor || kind > gsim::kPkStoreXor || B > 3 || op.data % 16) g_inconsistent = true;
+          if (kind == gsim::kPkLoadXor || kind > gsim::kPkStoreXor || (B > 3 && kind != gsim::kPkDiagN) ||
+              op.data % 16)
+            g_inconsistent = true;
           const bool on = (base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl;
           if (kind == gsim::kPkStoreXor) {
             if (on) sx ^= op.amask;
@@ -302,7 +304,9 @@ void apply_stage_pk(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &
               idx |= ((j >> B) & 1u) << op.dq;
               if (op.jidx[j] != (((j >> B) & 1u) << op.dq)) g_inconsistent = true;
             } else if (kind == gsim::kPkDiagN) {
-              idx |= op.jidx[j];
+              // the kernel reads the entry of the masked bits' value
+              if (op.jidx[j] != op.jidx[j & B] || __builtin_popcount(B) < 2) g_inconsistent = true;
+              idx |= op.jidx[j & B];
             } else if (op.jidx[j]) {
               g_inconsistent = true;
             }
