@@ -445,30 +445,48 @@ inline bool build_substages_pk(StagePlan &sp) {
   std::vector<char> done(nops, 0);
   size_t ndone = 0;
   while (ndone < nops) {
-    uint32_t R = 1u << P;
-    std::vector<size_t> chosen;
-    bool progress = true;
-    while (progress) {
-      progress = false;
-      for (size_t o = 0; o < nops; ++o) {
-        if (done[o]) continue;
-        bool ready = true;
-        for (size_t p : preds[o])
-          if (!done[p]) {
-            ready = false;
-            break;
-          }
-        if (!ready) continue;
-        if (sp.ops[o].kind == 0) {
-          if (unsigned(__builtin_popcount(R | tmask[o])) > 5) continue;
-          R |= tmask[o];
+    // The substage's register bits: of every set of 4 tile bits besides P,
+    // the one under which list scheduling takes the most operations now
+    // (ties: the first such set in enumeration order).
+    auto schedule = [&](uint32_t R, std::vector<char> &dn, std::vector<size_t> *chosen) {
+      size_t taken = 0;
+      bool progress = true;
+      while (progress) {
+        progress = false;
+        for (size_t o = 0; o < nops; ++o) {
+          if (dn[o]) continue;
+          if (sp.ops[o].kind == 0 && (tmask[o] & ~R)) continue;
+          bool ready = true;
+          for (size_t p : preds[o])
+            if (!dn[p]) {
+              ready = false;
+              break;
+            }
+          if (!ready) continue;
+          dn[o] = 1;
+          ++taken;
+          if (chosen) chosen->push_back(o);
+          progress = true;
         }
-        done[o] = 1;
-        ++ndone;
-        chosen.push_back(o);
-        progress = true;
+      }
+      return taken;
+    };
+    uint32_t R = 0;
+    size_t best_taken = 0;
+    for (uint32_t b = 0, k = 0; b < L && k < 4; ++b)  // a valid set whatever happens below
+      if (b != P) R |= 1u << b, ++k;
+    R |= 1u << P;
+    for (uint32_t cand = 0; cand < (1u << L); ++cand) {
+      if (((cand >> P) & 1) || __builtin_popcount(cand) != 4) continue;
+      std::vector<char> dn = done;
+      const size_t taken = schedule(cand | (1u << P), dn, nullptr);
+      if (taken > best_taken) {
+        best_taken = taken;
+        R = cand | (1u << P);
       }
     }
+    std::vector<size_t> chosen;
+    ndone += schedule(R, done, &chosen);
     // pad to 5 register bits, from the bank classes (pair-bit mod 3) with most spare bits
     while (unsigned(__builtin_popcount(R)) < 5) {
       int best = -1, best_count = -1;
@@ -761,39 +779,58 @@ class StagePlanner {
         done[first] = 1;
         continue;
       }
-      uint64_t local = low_mask();
-      uint64_t blocked = 0;
-      std::vector<size_t> placed;
-      size_t scanned = 0;
-      for (size_t i = first; i < gates.size() && scanned < window_; ++i) {
-        if (done[i]) continue;
-        ++scanned;
-        const Item &it = items[i];
-        if (it.touch & blocked) {
-          blocked |= it.touch;
-          continue;
-        }
-        if (it.wide) {
-          blocked |= it.touch;
-          continue;
-        }
-        if (!it.diag) {
-          const uint64_t nl = local | it.tmask;
-          if (unsigned(__builtin_popcountll(nl)) > L_) {
+      // Place gates for a stage with `cap` local bits for dense targets.
+      auto place = [&](unsigned cap, uint64_t &local) {
+        local = low_mask();
+        uint64_t blocked = 0;
+        std::vector<size_t> placed;
+        size_t scanned = 0;
+        for (size_t i = first; i < gates.size() && scanned < window_; ++i) {
+          if (done[i]) continue;
+          ++scanned;
+          const Item &it = items[i];
+          if (it.touch & blocked) {
             blocked |= it.touch;
             continue;
           }
-          local = nl;
+          if (it.wide) {
+            blocked |= it.touch;
+            continue;
+          }
+          if (!it.diag) {
+            const uint64_t nl = local | it.tmask;
+            if (unsigned(__builtin_popcountll(nl)) > cap) {
+              blocked |= it.touch;
+              continue;
+            }
+            local = nl;
+          }
+          placed.push_back(i);
         }
-        placed.push_back(i);
+        return placed;
+      };
+      uint64_t local = 0;
+      std::vector<size_t> placed = place(L_, local);
+      uint64_t touched = 0;
+      for (size_t i : placed) touched |= items[i].touch;
+      if (pack_ && L_ > m_ + 1 && !(fill_local_pack(local, touched) & ~touched)) {
+        // every local bit is a dense target of the stage and no qubit is free:
+        // place again with one local bit fewer, which leaves room for a pack bit
+        uint64_t local2 = 0;
+        std::vector<size_t> placed2 = place(L_ - 1, local2);
+        uint64_t touched2 = 0;
+        for (size_t i : placed2) touched2 |= items[i].touch;
+        if (!placed2.empty() && (fill_local_pack(local2, touched2) & ~touched2)) {
+          placed.swap(placed2);
+          local = local2;
+          touched = touched2;
+        }
       }
       for (size_t i : placed) done[i] = 1;
       steps.push_back(PlanStep{});
       PlanStep &st = steps.back();
       st.is_stage = true;
       st.ngates = uint32_t(placed.size());
-      uint64_t touched = 0;
-      for (size_t i : placed) touched |= items[i].touch;
       const uint64_t full = pack_ ? fill_local_pack(local, touched) : fill_local(local);
       build_stage(gates, items, placed, full, st.stage);
       if (pack_) st.stage.pack = choose_pack(st.stage, touched);
