@@ -694,20 +694,31 @@ def run_adjoint(a):
 
 def run_learned(a):
     """Learned fusion planner on a stream of random circuits (qubits uniform
-    in 20..30 complex64, depth 10..200, the config-5 gate mix, 10% ending
-    with the time evolution of a 50-term Pauli Hamiltonian): host wall time
-    with the shipped cost model against the greedy fixed-size fusion and the
-    stage planner, and 1 - F of the learned result against the greedy one;
+    in 20..32 complex64, depth 10..200, the config-5 gate mix, 10% ending
+    with the time evolution of a 50-term Pauli Hamiltonian, on states of up to
+    30 qubits): host wall time with the shipped cost model against the greedy
+    fixed-size fusion and the stage planner, the evolution method the learned
+    planner chose for each tail, and 1 - F of the learned result against the
+    greedy one;
     then the same comparison on block-local circuits (26-30 qubits), where the
     model's own tensor-core clusters compete with the stage plan."""
     from projectq_gb300 import costmodel
 
     shipped = costmodel.load()
     res = costmodel.evaluate(shipped["params"], shipped["regimes_c64"], ncirc=a.ngates, seed=11)
-    choices = {}
+    choices, tails = {}, {}
     for r in res["rows"]:
         choices[r["choice"]] = choices.get(r["choice"], 0) + 1
+        if r.get("tail"):
+            tails[r["tail_method"]] = tails.get(r["tail_method"], 0) + 1
     rows = res.pop("rows")
+    tail_rows = [r for r in rows if r.get("tail")]
+    res["time_evolution"] = {
+        "learned_methods": tails,
+        "greedy_s": sum(r["greedy_s"] - r["greedy_gates_s"] for r in tail_rows),
+        "learned_s": sum(r["learned_s"] - r["learned_gates_s"] for r in tail_rows),
+        "staged_s": sum(r["staged_s"] - r["staged_gates_s"] for r in tail_rows) if tail_rows and "staged_s" in tail_rows[0]
+        else None}
     blk = costmodel.evaluate_blocked(shipped["params"], shipped["regimes_c64"])
     blk_rows = blk.pop("rows")
 
