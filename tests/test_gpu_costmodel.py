@@ -168,13 +168,14 @@ def test_shipped_cost_model_beats_greedy_fusion():
 @pytest.mark.skipif(not cm.DATA.exists(), reason="no trained cost model shipped")
 def test_learned_planner_uses_its_clusters_on_block_local_circuits():
     """Where the network's choice differs from the stage plan: on a 30-qubit
-    circuit of 40-gate blocks over 7 neighbouring qubits it predicts its own
+    circuit of 80-gate blocks over 7 neighbouring qubits it predicts its own
     tensor-core clusters (one launch per block) to be faster, runs them, and
     is not slower than the stage plan in measured wall time (5% noise
-    allowed); the states agree."""
+    allowed); the states agree.  (With 40-gate blocks the two plans are
+    predicted within the planner's 10% margin, and it keeps the stage plan.)"""
     shipped = cm.load()
     n = 30
-    gates = cm.blocked_circuit(np.random.default_rng(3 * 1000 + n * 10 + 7), n, 7, 40)
+    gates = cm.blocked_circuit(np.random.default_rng(3 * 1000 + n * 10 + 7), n, 7, 80)
     t_staged, _, s_staged = cm.wall_time(n, gates, "staged", "c64", keep=True)
     t_learned, choice, s_learned = cm.wall_time(n, gates, "learned", "c64", shipped["params"],
                                                  shipped["regimes_c64"], keep=True)
