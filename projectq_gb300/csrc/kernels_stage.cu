@@ -587,9 +587,13 @@ __device__ __forceinline__ void swap1(f2 (&RE)[16], f2 (&IM)[16], uint32_t amask
 
 // (RE, IM) *= F with F = Fx + i Fy per half: RE' = Fx RE - Fy IM, IM' = Fx IM + Fy RE
 __device__ __forceinline__ void cmul(f2 &re, f2 &im, f2 fx, f2 fy, f2 fn) {
-  const f2 r = re;
-  re = fma2(fx, r, mul2(fn, im));
-  im = fma2(fx, im, mul2(fy, r));
+  // both products first: each output's last instruction is then the last use
+  // of its own input, and the result stays in that input's registers (with
+  // the other order ptxas moved about 20 registers per diagonal operation at
+  // the dispatch merge, and the kernel spilled)
+  const f2 t1 = mul2(fn, im), t2 = mul2(fy, re);
+  re = fma2(fx, re, t1);
+  im = fma2(fx, im, t2);
 }
 
 template <int B>
