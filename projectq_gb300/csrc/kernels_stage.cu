@@ -804,12 +804,12 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
       for (; o < S.op_end; ++o) {
         const PkOpDev &op = ops[o];
         const uint32_t code = op.code;
-        const bool on = (base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl;
-        if (code == kPkStoreXor) {
-          if (on) sx ^= op.amask;
+        // controls are tested only for operations that have them
+        if ((code & kPkCtl) && !((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl)) continue;
+        if ((code & 15u) == kPkStoreXor) {
+          sx ^= op.amask;
           continue;
         }
-        if (!on) continue;
         pk::apply_op(RE, IM, blob, op, code, row, base);
       }
       {

@@ -387,8 +387,13 @@ enum : uint32_t {
   kPkStoreXor = 6,  // X folded into the store addresses
 };
 
+// Operations with row or tile controls carry this flag in their code: the
+// kernel tests controls only for them.
+constexpr uint32_t kPkCtl = 1u << 13;
+
 struct alignas(16) PkOpDev {
-  uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12 (kPkDiagN: b is a pair-bit mask)
+  uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12 | kPkCtl (kPkDiagN: b is a pair-bit mask;
+                     // kPkLoadXor: the kind alone, its controls always tested)
   uint32_t data;     // blob offset of the operation's data (16-byte aligned)
   uint32_t amask;    // dense / swap with register controls: the register indices it pairs from (16 bits);
                      // folded X: the address XOR
@@ -734,7 +739,10 @@ inline bool build_substages_pk(StagePlan &sp) {
   const size_t head = subs_bytes + ops_bytes;
   if (head + data.size() > kPkBlobMax) return false;
   for (PkSubDev &d : dsubs) d.tab += uint32_t(head);
-  for (PkOpDev &d : dops) d.data += uint32_t(head);
+  for (PkOpDev &d : dops) {
+    d.data += uint32_t(head);
+    if (d.code != kPkLoadXor && (d.gctrl || d.tctrl)) d.code |= kPkCtl;
+  }
   sp.pk.assign(head + data.size(), 0);
   std::memcpy(sp.pk.data(), dsubs.data(), dsubs.size() * sizeof(PkSubDev));
   std::memcpy(sp.pk.data() + subs_bytes, dops.data(), ops_bytes);

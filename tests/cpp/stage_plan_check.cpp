@@ -252,7 +252,9 @@ void apply_stage_pk(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &
           if (kind == gsim::kPkLoadXor || kind > gsim::kPkStoreXor || (B > 3 && kind != gsim::kPkDiagN) ||
               op.data % 16)
             g_inconsistent = true;
-          const bool on = (base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl;
+          // the kernel tests controls only under the flag, so the flag must mark every controlled operation
+          if (((op.code & gsim::kPkCtl) != 0) != (op.gctrl != 0 || op.tctrl != 0)) g_inconsistent = true;
+          const bool on = !(op.code & gsim::kPkCtl) || ((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl);
           if (kind == gsim::kPkStoreXor) {
             if (on) sx ^= op.amask;
             continue;
