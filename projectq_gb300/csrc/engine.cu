@@ -110,8 +110,10 @@ class Engine {
     for (DevBuf *b : {&state_, &scratch_, &part_, &small_, &aux1_, &aux2_, &aux3_, &table_, &table2_, &upload_dev_})
       b->release();
     pinned_.release();
-    upload_host_.release();
-    if (upload_ev_) cudaEventDestroy(upload_ev_);
+    for (int k = 0; k < kUploadSlots; ++k) {
+      upload_host_[k].release();
+      if (upload_ev_[k]) cudaEventDestroy(upload_ev_[k]);
+    }
     for (UploadSlot &sl : mslots_) {
       sl.dev.release();
       sl.host.release();
@@ -1094,8 +1096,10 @@ class Engine {
   }
 
   void run_staged();
+  std::vector<PlanStep> plan_stages(const std::vector<StageGate> &gates) const;
+  void build_stage_data(StagePlan &sp) const;
   std::vector<PlanStep> plan_staged(const std::vector<StageGate> &gates) const;
-  void execute_staged(std::vector<PlanStep> &steps);
+  void execute_staged(std::vector<PlanStep> &steps, bool build = false);
   void exec_stage(const StagePlan &sp, const void *d_ops, const void *d_pool);
   void run_learned();
   std::vector<StageGate> queued_positions() const;
@@ -1248,8 +1252,13 @@ class Engine {
   std::unordered_map<uint64_t, double> memo_;  // launch key -> predicted ms
   double last_pred_[3] = {0, 0, 0};                // predicted ms: greedy, staged, learned clusters
   DevBuf upload_dev_;
-  HostBuf upload_host_;
-  cudaEvent_t upload_ev_ = nullptr;
+  // Page-locked staging of stage uploads, a ring of slots: a flush's copies
+  // run in stream order between its launches, so a slot is written again
+  // only after the copies of the flush that used it kUploadSlots flushes ago.
+  static constexpr int kUploadSlots = 4;
+  HostBuf upload_host_[kUploadSlots];
+  cudaEvent_t upload_ev_[kUploadSlots] = {};
+  int upload_slot_ = 0;
   uint64_t counters_[7] = {0, 0, 0, 0, 0, 0, 0};
   // timing
   cudaEvent_t timer_[16] = {};
@@ -1368,7 +1377,9 @@ uint64_t Engine::sample(double rnd) {
   return pick - 1;
 }
 
-std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) const {
+// The stages of `gates`: which gates run in which pass, their tile bits and
+// merged operations (StagePlanner); the kernels' substage data comes after.
+std::vector<PlanStep> Engine::plan_stages(const std::vector<StageGate> &gates) const {
   // Tiles of 2^(r + 8) amplitudes (64 KB complex64, 32 KB complex128), with
   // runs of 2^5 / 2^4 contiguous amplitudes (256 bytes) in HBM.
   const unsigned L = prec_ == GSIM_C64 ? tile_bits_c64_ : tile_bits_c128_;
@@ -1376,88 +1387,106 @@ std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) c
   // complex64 stages get a pack bit where possible (the packed-pair kernel)
   const bool pk = prec_ == GSIM_C64 && stage_kernel_ == 2;
   StagePlanner planner(N_, L, m, 512, pk);
-  std::vector<PlanStep> steps = planner.plan(gates);
-  // Register substages where the tile is 2^(r + 8) amplitudes (256 threads).
+  return planner.plan(gates);
+}
+
+// A stage's substages for its kernel: packed pairs (complex64, with a pack
+// bit), else register substages where the tile is 2^(r + 8) amplitudes (256
+// threads), else none (the pass kernel).
+void Engine::build_stage_data(StagePlan &sp) const {
   const unsigned r = prec_ == GSIM_C64 ? kRegBitsC64 : kRegBitsC128, rho = prec_ == GSIM_C64 ? 4 : 3;
-  for (auto &st : steps) {
-    if (!(st.is_stage && stage_kernel_ >= 1 && st.stage.L == r + 8)) continue;
-    if (pk && build_substages_pk(st.stage)) continue;
-    build_substages(st.stage, r, rho);
-    if (stage_subs_bytes(st.stage) + st.stage.sops.size() * sizeof(SubOpDev) > kStageTableBytes) {
-      st.stage.subs.clear();  // descriptors too large for the kernel parameter
-      st.stage.sops.clear();
-    }
+  if (!(stage_kernel_ >= 1 && sp.L == r + 8)) return;
+  if (prec_ == GSIM_C64 && stage_kernel_ == 2 && build_substages_pk(sp)) return;
+  build_substages(sp, r, rho);
+  if (stage_subs_bytes(sp) + sp.sops.size() * sizeof(SubOpDev) > kStageTableBytes) {
+    sp.subs.clear();  // descriptors too large for the kernel parameter
+    sp.sops.clear();
   }
+}
+
+std::vector<PlanStep> Engine::plan_staged(const std::vector<StageGate> &gates) const {
+  std::vector<PlanStep> steps = plan_stages(gates);
+  for (auto &st : steps)
+    if (st.is_stage) build_stage_data(st.stage);
   return steps;
 }
 
+// The queued gates as stages, each stage's substages built just before its
+// launch: the host builds stage k + 1 while the GPU runs stage k.
 void Engine::run_staged() {
   if (queue_.empty()) return;
   std::vector<StageGate> gates = queued_positions();
   queue_.clear();
-  std::vector<PlanStep> steps = plan_staged(gates);
-  execute_staged(steps);
+  std::vector<PlanStep> steps = plan_stages(gates);
+  execute_staged(steps, true);
 }
 
-void Engine::execute_staged(std::vector<PlanStep> &steps) {
-  // Serialise every stage's operations and matrices into one upload.
+// Launch the steps in order.  Every stage's descriptors, tables and matrices
+// go to their own slice of one page-locked staging buffer and are copied by
+// their own cudaMemcpyAsync right before the stage's launch; the buffer is
+// sized up front by an upper bound per stage (the substage data is at most
+// kPkBlobMax / kStageTableBytes / the operation array, plus the matrices).
+// build: the stages' substages are built here, one stage at a time.
+void Engine::execute_staged(std::vector<PlanStep> &steps, bool build) {
   const size_t esz = bpa_;
-  size_t bytes = 0;
-  std::vector<size_t> off_ops(steps.size()), off_pool(steps.size());
-  for (size_t i = 0; i < steps.size(); ++i) {
-    if (!steps[i].is_stage) continue;
-    const StagePlan &sp = steps[i].stage;
-    off_ops[i] = bytes;
-    if (!sp.pk.empty()) {  // the packed-pair blob carries its own data
-      bytes += (sp.pk.size() + 15) / 16 * 16;
-      off_pool[i] = bytes;
+  auto round16 = [](size_t n) { return (n + 15) / 16 * 16; };
+  size_t bound = 0;
+  for (auto const &st : steps) {
+    if (!st.is_stage) continue;
+    const StagePlan &sp = st.stage;
+    bound += std::max({kPkBlobMax, kStageTableBytes, round16(sp.ops.size() * sizeof(StageOpDev))}) +
+             round16(sp.pool.size() * esz);
+  }
+  char *host = nullptr, *dev = nullptr;
+  if (bound) {
+    upload_slot_ = (upload_slot_ + 1) % kUploadSlots;
+    if (upload_ev_[upload_slot_]) CK(cudaEventSynchronize(upload_ev_[upload_slot_]));  // the slot is free again
+    host = static_cast<char *>(upload_host_[upload_slot_].get(bound));
+    dev = static_cast<char *>(upload_dev_.get(bound));
+  }
+  size_t off = 0;
+  for (auto &st : steps) {
+    if (!st.is_stage) {
+      exec_dense(st.dense);
       continue;
     }
-    if (!sp.subs.empty())
-      bytes += stage_subs_bytes(sp) + (sp.sops.size() * sizeof(SubOpDev) + 15) / 16 * 16;
-    else
-      bytes += (sp.ops.size() * sizeof(StageOpDev) + 15) / 16 * 16;
-    off_pool[i] = bytes;  // for register stages the pool directly follows the operations
-    bytes += (sp.pool.size() * esz + 15) / 16 * 16;
-  }
-  char *dev = nullptr;
-  if (bytes) {
-    if (upload_ev_) CK(cudaEventSynchronize(upload_ev_));  // the staging buffer is free again
-    char *host = static_cast<char *>(upload_host_.get(bytes));
-    for (size_t i = 0; i < steps.size(); ++i) {
-      if (!steps[i].is_stage) continue;
-      const StagePlan &sp = steps[i].stage;
-      if (!sp.pk.empty()) {
-        std::memcpy(host + off_ops[i], sp.pk.data(), sp.pk.size());
-        continue;
-      }
+    StagePlan &sp = st.stage;
+    if (build) build_stage_data(sp);
+    const size_t o = off;
+    size_t pool = 0;
+    if (!sp.pk.empty()) {  // the packed-pair blob carries its own data
+      std::memcpy(host + o, sp.pk.data(), sp.pk.size());
+      off += round16(sp.pk.size());
+      pool = off;
+    } else {
       if (!sp.subs.empty()) {
-        std::memcpy(host + off_ops[i], sp.subs.data(), sp.subs.size() * sizeof(SubstageDev));
-        std::memcpy(host + off_ops[i] + stage_subs_bytes(sp), sp.sops.data(), sp.sops.size() * sizeof(SubOpDev));
+        std::memcpy(host + o, sp.subs.data(), sp.subs.size() * sizeof(SubstageDev));
+        std::memcpy(host + o + stage_subs_bytes(sp), sp.sops.data(), sp.sops.size() * sizeof(SubOpDev));
+        off += stage_subs_bytes(sp) + round16(sp.sops.size() * sizeof(SubOpDev));
       } else {
-        std::memcpy(host + off_ops[i], sp.ops.data(), sp.ops.size() * sizeof(StageOpDev));
+        std::memcpy(host + o, sp.ops.data(), sp.ops.size() * sizeof(StageOpDev));
+        off += round16(sp.ops.size() * sizeof(StageOpDev));
       }
+      pool = off;  // for register stages the pool directly follows the operations
       if (prec_ == GSIM_C64) {
-        float *f = reinterpret_cast<float *>(host + off_pool[i]);
+        float *f = reinterpret_cast<float *>(host + pool);
         for (size_t j = 0; j < sp.pool.size(); ++j) {
           f[2 * j] = float(sp.pool[j].real());
           f[2 * j + 1] = float(sp.pool[j].imag());
         }
       } else {
-        std::memcpy(host + off_pool[i], sp.pool.data(), sp.pool.size() * 16);
+        std::memcpy(host + pool, sp.pool.data(), sp.pool.size() * 16);
       }
+      off += round16(sp.pool.size() * esz);
     }
-    dev = static_cast<char *>(upload_dev_.get(bytes));
-    CK(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, stream_));
-    if (!upload_ev_) CK(cudaEventCreateWithFlags(&upload_ev_, cudaEventDisableTiming));
-    CK(cudaEventRecord(upload_ev_, stream_));
+    if (off > bound) fail(GSIM_ERR_RUNTIME, "stage upload larger than its bound");
+    CK(cudaMemcpyAsync(dev + o, host + o, off - o, cudaMemcpyHostToDevice, stream_));
+    exec_stage(sp, dev + o, dev + pool);
   }
-  for (size_t i = 0; i < steps.size(); ++i) {
-    if (!steps[i].is_stage) {
-      exec_dense(steps[i].dense);
-      continue;
-    }
-    exec_stage(steps[i].stage, dev + off_ops[i], dev + off_pool[i]);
+  if (bound) {
+    cudaEvent_t &ev = upload_ev_[upload_slot_];
+    if (!ev) CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, stream_));
   }
 }
 

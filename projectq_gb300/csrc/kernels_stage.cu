@@ -643,32 +643,35 @@ __device__ __forceinline__ void dense1_cls(f2 (&RE)[16], f2 (&IM)[16], const f2 
 }
 
 __device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsigned char *__restrict__ blob,
-                                         const PkOpDev &op, uint32_t code, uint32_t row, uint64_t base) {
+                                         const PkOpDev &op, uint32_t code, uint32_t row, uint64_t base,
+                                         uint32_t &sx) {
   const uint32_t kind = code & 15u, B = (code >> 4) & 15u;
-  if (kind == kPkDense) {
+  if (kind <= kPkSwap) {  // dense or swap on register pair-bit B: one indexed branch
     const f2 *M = reinterpret_cast<const f2 *>(blob + op.data);
     const uint32_t cls = (code >> 8) & 15u;
     const bool masked = (code >> 12) & 1u;
-    switch (B) {
+    switch (kind * 4 + B) {
       case 0: dense1_cls<0>(RE, IM, M, op.amask, cls, masked); break;
       case 1: dense1_cls<1>(RE, IM, M, op.amask, cls, masked); break;
       case 2: dense1_cls<2>(RE, IM, M, op.amask, cls, masked); break;
-      default: dense1_cls<3>(RE, IM, M, op.amask, cls, masked); break;
-    }
-    return;
-  }
-  if (kind == kPkSwap) {
-    switch (B) {
-      case 0: swap1<0>(RE, IM, op.amask); break;
-      case 1: swap1<1>(RE, IM, op.amask); break;
-      case 2: swap1<2>(RE, IM, op.amask); break;
+      case 3: dense1_cls<3>(RE, IM, M, op.amask, cls, masked); break;
+      case 4: swap1<0>(RE, IM, op.amask); break;
+      case 5: swap1<1>(RE, IM, op.amask); break;
+      case 6: swap1<2>(RE, IM, op.amask); break;
       default: swap1<3>(RE, IM, op.amask); break;
     }
     return;
   }
+  if (kind == kPkStoreXor) {
+    sx ^= op.amask;
+    return;
+  }
   // diagonal: table index bits of the row and non-local qubits
   uint32_t cidx = 0;
-  for (uint32_t i = 0; i < op.nsrc; ++i) {
+  const uint32_t nsrc = op.nsrc;  // at most 6: a merged diagonal spans at most 6 qubits
+#pragma unroll
+  for (uint32_t i = 0; i < 6; ++i) {
+    if (i >= nsrc) break;
     const uint32_t sidx = op.src[i];
     const uint32_t bit = (sidx & 0x80u) ? uint32_t((base >> (sidx & 0x7Fu)) & 1u) : (row >> sidx) & 1u;
     cidx |= bit << op.sbit[i];
@@ -806,11 +809,7 @@ __global__ void __launch_bounds__(256, 2) stage_pk_kernel(float2 *__restrict__ p
         const uint32_t code = op.code;
         // controls are tested only for operations that have them
         if ((code & kPkCtl) && !((base & op.gctrl) == op.gctrl && (row & op.tctrl) == op.tctrl)) continue;
-        if ((code & 15u) == kPkStoreXor) {
-          sx ^= op.amask;
-          continue;
-        }
-        pk::apply_op(RE, IM, blob, op, code, row, base);
+        pk::apply_op(RE, IM, blob, op, code, row, base, sx);
       }
       {
         const uint4 *st = reinterpret_cast<const uint4 *>(tab + 272);
