@@ -694,9 +694,9 @@ def run_adjoint(a):
 
 def run_learned(a):
     """Learned fusion planner on a stream of random circuits (qubits uniform
-    in 20..32 complex64, depth 10..200, the config-5 gate mix, 10% ending
-    with the time evolution of a 50-term Pauli Hamiltonian, on states of up to
-    30 qubits): host wall time with the shipped cost model against the greedy
+    in 20..32 complex64, depth 10..200, the gate mix of
+    costmodel.random_circuit, 10% ending with the time evolution of a 50-term
+    Pauli Hamiltonian, on states of up to 30 qubits): host wall time with the shipped cost model against the greedy
     fixed-size fusion and the stage planner, the evolution method the learned
     planner chose for each tail, and 1 - F of the learned result against the
     greedy one;

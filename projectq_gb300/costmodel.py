@@ -357,7 +357,7 @@ def calibrate(params, per_size=3, sizes=range(18, 33), precisions=("c64", "c128"
 
 def evaluate(params, regimes, ncirc, seed=1, nmin=20, nmax=32, dmin=10, dmax=200, precision="c64",
              with_staged=True, fidelity=True):
-    """Config-5 style stream of `ncirc` random circuits (10% end with the time
+    """A stream of `ncirc` random circuits (random_circuit; 10% end with the time
     evolution of a 50-term Pauli Hamiltonian): wall time with the learned
     planner against the greedy fixed-size fusion (and the stage planner), and
     1 - F between the learned and the greedy final states.  The totals
