@@ -316,13 +316,13 @@ def run_reference(a):
     `--ref-gates` consecutive gates (the windows advance through the circuit,
     so K steps time K x window gates) in both of the reference's modes; the
     value is the faster mode's gates/s over the timed steps."""
-    from projectq_gb300.workloads import config2_circuit
+    from projectq_gb300.workloads import random_gate_circuit
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     set_omp_env()
-    gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
+    gates = random_gate_circuit(a.qubits, a.depth, a.per_layer, seed=0)
     nq = cpu_nq(a.qubits)
     eng = CpuEngine(nq)
     S = a.ref_gates
@@ -362,9 +362,9 @@ def accuracy_vs_reference(nq, depth, per_layer, fusion):
     sys.path.insert(0, str(ROOT / "tests"))
     from _backends import make, ref_api
     from projectq_gb300 import Simulator
-    from projectq_gb300.workloads import config2_circuit, random_state
+    from projectq_gb300.workloads import random_gate_circuit, random_state
 
-    gates = config2_circuit(nq, depth, per_layer, seed=0)
+    gates = random_gate_circuit(nq, depth, per_layer, seed=0)
     psi0 = random_state(nq, seed=0, dtype=np.complex128)
     ids = list(range(nq))
     kind = "reference engine (simulator.hpp), its own gate fusion" if ref_api() is not None else "oracle port"
@@ -397,9 +397,9 @@ def accuracy_vs_reference(nq, depth, per_layer, fusion):
 def run_only(a):
     """Profiling mode: the circuit on one precision, from |0...0> or psi0."""
     from projectq_gb300 import Simulator
-    from projectq_gb300.workloads import config2_circuit, random_state
+    from projectq_gb300.workloads import random_gate_circuit, random_state
 
-    gates = config2_circuit(a.qubits, a.depth, a.per_layer, seed=0)
+    gates = random_gate_circuit(a.qubits, a.depth, a.per_layer, seed=0)
     sim = Simulator(1, precision=a.only, fusion=a.fusion)
     sim.set_stage_kernel(a.stage_kernel)
     for q in range(a.qubits):
@@ -837,11 +837,11 @@ def main():
     dist, world, rank, local = dist_init()
     from projectq_gb300 import Simulator
     from projectq_gb300.simulator import pin_host, set_device
-    from projectq_gb300.workloads import config2_circuit, random_state
+    from projectq_gb300.workloads import random_gate_circuit, random_state
 
     set_device(local)
     nq = a.qubits
-    gates = config2_circuit(nq, a.depth, a.per_layer, seed=0)
+    gates = random_gate_circuit(nq, a.depth, a.per_layer, seed=0)
     G = len(gates)
     psi0 = random_state(nq, seed=0, dtype=np.complex64)
     h2d_bytes = int(psi0.nbytes)

@@ -35,7 +35,7 @@ def Rz(t):  # noqa: N802
     return np.array([[np.exp(-0.5j * t), 0], [0, np.exp(0.5j * t)]], dtype=np.complex128)
 
 
-def config1_circuit(n=20, depth=20, seed=0):
+def layered_rotation_circuit(n=20, depth=20, seed=0):
     """Layered circuit: Rx, Ry, Rz on every qubit (angles U[0, 2pi) drawn in
     layer -> qubit -> gate order from numpy default_rng(seed)), then CNOT
     (i -> i+1) for i = 0, 2, ... on even layers and 1, 3, ... on odd ones."""
@@ -52,10 +52,10 @@ def config1_circuit(n=20, depth=20, seed=0):
     return gates
 
 
-CONFIG2_KINDS = ("H", "T", "S", "Rx", "Ry", "Rz", "CNOT", "CZ", "Toffoli")
+RANDOM_GATE_KINDS = ("H", "T", "S", "Rx", "Ry", "Rz", "CNOT", "CZ", "Toffoli")
 
 
-def config2_circuit(n=30, depth=40, per_layer=40, seed=0):
+def random_gate_circuit(n=30, depth=40, per_layer=40, seed=0):
     """Random circuit: each layer has `per_layer` gates drawn uniformly from
     {H, T, S, Rx, Ry, Rz (theta ~ U[0, 2pi)), CNOT and CZ on a random pair,
     Toffoli on a random triple (2 controls)}, all on uniformly random qubits."""
@@ -63,7 +63,7 @@ def config2_circuit(n=30, depth=40, per_layer=40, seed=0):
     gates = []
     for _ in range(depth):
         for _ in range(per_layer):
-            kind = CONFIG2_KINDS[int(rng.integers(len(CONFIG2_KINDS)))]
+            kind = RANDOM_GATE_KINDS[int(rng.integers(len(RANDOM_GATE_KINDS)))]
             if kind in ("H", "T", "S"):
                 q = int(rng.integers(n))
                 gates.append(({"H": H, "T": T, "S": S}[kind], (q,), ()))

@@ -11,11 +11,11 @@ committed and are what the tests compare against everywhere else.
     python tests/golden/make_golden.py
 
 Fixtures (numpy .npz):
-  config1_n10.npz  the layered Rx/Ry/Rz + CNOT circuit (10 qubits, depth 10,
+  layered_n10.npz  the layered Rx/Ry/Rz + CNOT circuit (10 qubits, depth 10,
                    seed 0): full final state with a run() per gate and with the
                    reference's fusion, <Z0 Z1 + X5 X6>, 8 measurement draws of
                    the engine RNG (seed 0), each on a fresh copy of the state.
-  config1_n20.npz  the same circuit at 20 qubits, depth 20 (the workload the
+  layered_n20.npz  the same circuit at 20 qubits, depth 20 (the workload the
                    reference numbers are quoted on): 4096 sampled amplitudes,
                    per-qubit probabilities, <Z0 Z1 + X5 X6>, 8 draws.
   ops_small.npz    every other entry point on small seeded inputs: a mixed
@@ -38,15 +38,15 @@ sys.path.insert(0, str(HERE.parent))
 
 from _backends import REF_LIB, make  # noqa: E402
 from _circuits import allocate, random_mixed_circuit, random_pauli_sum, run_circuit  # noqa: E402
-from projectq_gb300.workloads import config1_circuit, random_state  # noqa: E402
+from projectq_gb300.workloads import layered_rotation_circuit, random_state  # noqa: E402
 
 ZZ_XX = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
 
 
-def config1(n, depth, fused):
+def layered(n, depth, fused):
     sim = make("ref", seed=0)
     allocate(sim, n)
-    run_circuit(sim, config1_circuit(n, depth, seed=0), run_each=not fused)
+    run_circuit(sim, layered_rotation_circuit(n, depth, seed=0), run_each=not fused)
     return sim
 
 
@@ -65,31 +65,31 @@ def draws(sim, n, count=8):
     return np.array(out, dtype=np.int64)
 
 
-def make_config1_n10():
+def make_layered_n10():
     n, depth = 10, 10
     res = {}
     for fused in (False, True):
-        sim = config1(n, depth, fused)
+        sim = layered(n, depth, fused)
         tag = "fused" if fused else "unfused"
         res["state_" + tag] = sim.cheat()[1]
         res["zz_xx_" + tag] = sim.get_expectation_value(ZZ_XX, list(range(n)))
         res["draws_" + tag] = draws(sim, n)
-    np.savez_compressed(HERE / "config1_n10.npz", **res)
+    np.savez_compressed(HERE / "layered_n10.npz", **res)
 
 
-def make_config1_n20():
+def make_layered_n20():
     n, depth = 20, 20
     idx = np.sort(np.random.default_rng(0).choice(1 << n, size=4096, replace=False))
     res = {"sample_index": idx}
     for fused in (False, True):
-        sim = config1(n, depth, fused)
+        sim = layered(n, depth, fused)
         tag = "fused" if fused else "unfused"
         psi = sim.cheat()[1]
         res["sample_" + tag] = psi[idx]
         res["zz_xx_" + tag] = sim.get_expectation_value(ZZ_XX, list(range(n)))
         res["p1_" + tag] = np.array([sim.get_probability([1], [q]) for q in range(n)])
         res["draws_" + tag] = draws(sim, n)
-    np.savez_compressed(HERE / "config1_n20.npz", **res)
+    np.savez_compressed(HERE / "layered_n20.npz", **res)
 
 
 MATH_OPS = [
@@ -183,8 +183,8 @@ def main():
         subprocess.run(["bash", str(ROOT / "oracle" / "build_ref.sh")], check=True)
     if not REF_LIB.exists():
         sys.exit("the reference tree is needed to build oracle/_ref/libref_sim.so")
-    make_config1_n10()
-    make_config1_n20()
+    make_layered_n10()
+    make_layered_n20()
     make_ops()
     for f in sorted(HERE.glob("*.npz")):
         print(f.name, f.stat().st_size)

@@ -12,7 +12,7 @@ import pytest
 
 from _backends import make
 from _circuits import allocate, random_mixed_circuit, random_pauli_sum, run_circuit
-from projectq_gb300.workloads import H, X, config1_circuit, random_state
+from projectq_gb300.workloads import H, X, layered_rotation_circuit, random_state
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 sys.path.insert(0, str(GOLDEN))
@@ -34,11 +34,11 @@ def draws(sim, n, count=8):
 
 @pytest.mark.parametrize("prec", ["c128", "c64"])
 @pytest.mark.parametrize("fusion", ["reference", "none", "staged"])
-def test_config1_n20(prec, fusion):
-    g = np.load(GOLDEN / "config1_n20.npz")
+def test_layered_n20(prec, fusion):
+    g = np.load(GOLDEN / "layered_n20.npz")
     sim = make("gpu", seed=0, precision=prec, fusion=fusion)
     allocate(sim, 20)
-    run_circuit(sim, config1_circuit(20, 20, seed=0))
+    run_circuit(sim, layered_rotation_circuit(20, 20, seed=0))
     psi = sim.cheat()[1]
     assert np.max(np.abs(psi[g["sample_index"]] - g["sample_fused"])) < TOL[prec] * 10
     zz = sim.get_expectation_value(ZZ_XX, list(range(20)))
@@ -50,12 +50,12 @@ def test_config1_n20(prec, fusion):
 
 
 @pytest.mark.parametrize("fused", [False, True])
-def test_config1_n10_full_state(fused):
-    g = np.load(GOLDEN / "config1_n10.npz")
+def test_layered_n10_full_state(fused):
+    g = np.load(GOLDEN / "layered_n10.npz")
     tag = "fused" if fused else "unfused"
     sim = make("gpu", seed=0)
     allocate(sim, 10)
-    run_circuit(sim, config1_circuit(10, 10, seed=0), run_each=not fused)
+    run_circuit(sim, layered_rotation_circuit(10, 10, seed=0), run_each=not fused)
     assert np.max(np.abs(sim.cheat()[1] - g["state_" + tag])) < 1e-13
     assert draws(sim, 10) == list(g["draws_" + tag])
 

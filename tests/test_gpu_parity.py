@@ -370,10 +370,10 @@ def test_headline_circuit_precision_form():
     reductions (stage planner) against the complex128 path and the CPU oracle:
     1 - F <= 1e-6 (the stated bar; measured ~1e-12) and expectation values
     within 1e-6."""
-    from projectq_gb300.workloads import config2_circuit
+    from projectq_gb300.workloads import random_gate_circuit
 
     n = 20
-    gates = config2_circuit(n, depth=40, per_layer=40, seed=0)
+    gates = random_gate_circuit(n, depth=40, per_layer=40, seed=0)
     psi0 = random_state(n, seed=0)
     states, ev = {}, {}
     zz = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
@@ -436,9 +436,9 @@ def test_stage_kernels_against_oracle(n, mode):
     """The staged planner's three complex64 stage kernels on the headline
     circuit family plus controlled 1-qubit gates (register, row and
     non-local controls) against the oracle: max |d psi| 1e-5 (complex64)."""
-    from projectq_gb300.workloads import config2_circuit
+    from projectq_gb300.workloads import random_gate_circuit
 
-    gates = config2_circuit(n, depth=10, per_layer=n, seed=n)
+    gates = random_gate_circuit(n, depth=10, per_layer=n, seed=n)
     rng = np.random.default_rng(n)
     for g in random_mixed_circuit(n, 50, n + 1, kmax=1, max_ctrl=3):
         gates.insert(int(rng.integers(len(gates) + 1)), g)

@@ -12,7 +12,7 @@ import pytest
 import _refsuite
 from _backends import make
 from _circuits import allocate, random_mixed_circuit, random_pauli_sum, run_circuit
-from projectq_gb300.workloads import H, X, config1_circuit, mt19937_uniform, random_state
+from projectq_gb300.workloads import H, X, layered_rotation_circuit, mt19937_uniform, random_state
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
 ZZ_XX = [([(0, "Z"), (1, "Z")], 1.0), ([(5, "X"), (6, "X")], 1.0)]
@@ -29,22 +29,22 @@ def draws(sim, n, count=8):
 
 
 @pytest.mark.parametrize("fused", [False, True])
-def test_config1_n10_matches_reference_fixture(fused):
-    g = np.load(GOLDEN / "config1_n10.npz")
+def test_layered_n10_matches_reference_fixture(fused):
+    g = np.load(GOLDEN / "layered_n10.npz")
     tag = "fused" if fused else "unfused"
     sim = make("oracle", seed=0)
     allocate(sim, 10)
-    run_circuit(sim, config1_circuit(10, 10, seed=0), run_each=not fused)
+    run_circuit(sim, layered_rotation_circuit(10, 10, seed=0), run_each=not fused)
     assert np.max(np.abs(sim.cheat()[1] - g["state_" + tag])) < 1e-13
     assert sim.get_expectation_value(ZZ_XX, list(range(10))) == pytest.approx(float(g["zz_xx_" + tag]), abs=1e-13)
     assert draws(sim, 10) == list(g["draws_" + tag])
 
 
-def test_config1_n20_matches_reference_fixture():
-    g = np.load(GOLDEN / "config1_n20.npz")
+def test_layered_n20_matches_reference_fixture():
+    g = np.load(GOLDEN / "layered_n20.npz")
     sim = make("oracle", seed=0)
     allocate(sim, 20)
-    run_circuit(sim, config1_circuit(20, 20, seed=0))
+    run_circuit(sim, layered_rotation_circuit(20, 20, seed=0))
     psi = sim.cheat()[1]
     assert np.max(np.abs(psi[g["sample_index"]] - g["sample_fused"])) < 1e-13
     # the value quoted for this workload in the baseline notes: -0.108758128291

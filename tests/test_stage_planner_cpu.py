@@ -16,7 +16,7 @@ import pytest
 
 from _backends import make
 from _circuits import allocate, random_mixed_circuit, run_circuit
-from projectq_gb300.workloads import H, X, Z, config2_circuit, random_state
+from projectq_gb300.workloads import H, X, Z, random_gate_circuit, random_state
 
 HERE = Path(__file__).resolve().parent
 SRC = HERE / "cpp" / "stage_plan_check.cpp"
@@ -73,7 +73,7 @@ def test_planned_stages_equal_gate_by_gate(lib, n, L, m, seed, r, rho):
 
 def test_random_circuit_packs_many_gates_per_stage(lib):
     n = 14
-    gates = config2_circuit(n, depth=10, per_layer=14, seed=3)
+    gates = random_gate_circuit(n, depth=10, per_layer=14, seed=3)
     psi = random_state(n, seed=3)
     got, nst = plan_apply(lib, n, 12, 5, gates, psi, r=4, rho=4)
     exp = oracle_apply(n, gates, psi)
@@ -171,7 +171,7 @@ def test_packed_pair_stages_equal_gate_by_gate(lib, n, seed, avoid, kind, dense2
     k = len(keep)
     # (a one-tile state holds the whole circuit in one stage: kept small enough
     # for the kernel's shared-memory budget)
-    gates = relabel(config2_circuit(k, depth=12 if n > 13 else 4, per_layer=k, seed=seed))
+    gates = relabel(random_gate_circuit(k, depth=12 if n > 13 else 4, per_layer=k, seed=seed))
     gates = _sprinkle(gates, relabel(random_mixed_circuit(k, 60 if n > 13 else 20, seed + 10, kmax=1, max_ctrl=3)),
                       seed)
     if dense2:
