@@ -176,17 +176,54 @@ __global__ void __launch_bounds__(256) shrink_kernel(const cplx_t<T> *__restrict
     dst[j] = src[insert_zeros(j, &p, 1) + add];
 }
 
-// Measurement: per block of 2^lb amplitudes, the FP64 sum of |psi_i|^2.
+// Measurement: per block of 2^lb amplitudes, the sum of |psi_i|^2.  Its uses
+// are the approximate running sum that picks each block's candidate binades
+// and the exact test "every amplitude of the block is 0".  complex128: FP64.
+// complex64: FP32 (GB300's FP64 pipe made this pass several times longer than
+// reading the state), with a block of nonzero amplitudes whose FP32 sum
+// underflows reported as the smallest positive double, so the zero test stays
+// exact; a candidate that misses only sends the block to the element loop.
 template <typename T>
 __global__ void __launch_bounds__(256) block_norm_sums_kernel(const cplx_t<T> *__restrict__ psi,
                                                               uint64_t n, unsigned lb,
                                                               double *sums) {
   const uint64_t b0 = uint64_t(blockIdx.x) << lb;
   const uint64_t b1 = min(n, b0 + (uint64_t(1) << lb));
-  double s = 0.;
-  for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += norm2_fp64(psi[i]);
-  s = block_sum(s);
-  if (threadIdx.x == 0) sums[blockIdx.x] = s;
+  if constexpr (sizeof(T) == 4) {
+    __shared__ float ws[8];
+    __shared__ unsigned wn[8];
+    float s = 0.f;
+    unsigned nz = 0;
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+      const float2 z = psi[i];
+      s = fmaf(z.x, z.x, fmaf(z.y, z.y, s));
+      nz |= (__float_as_uint(z.x) | __float_as_uint(z.y)) << 1;  // sign bits out: -0 is 0
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      s += __shfl_down_sync(0xffffffffu, s, o);
+      nz |= __shfl_down_sync(0xffffffffu, nz, o);
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) {
+      ws[w] = s;
+      wn[w] = nz;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      float t = 0.f;
+      unsigned any = 0;
+      for (int k = 0; k < int(blockDim.x >> 5); ++k) {
+        t += ws[k];
+        any |= wn[k];
+      }
+      sums[blockIdx.x] = t > 0.f || t != t ? double(t) : (any ? 4.9406564584124654e-324 : 0.);
+    }
+  } else {
+    double s = 0.;
+    for (uint64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) s += norm2_fp64(psi[i]);
+    s = block_sum(s);
+    if (threadIdx.x == 0) sums[blockIdx.x] = s;
+  }
 }
 
 // x / 2^(e-52) rounded to nearest as an integer; flags bit 0 = exact tie,
