@@ -139,9 +139,9 @@ class ClockSampler:
 KERNEL_KINDS = ["dense_gate", "stage", "wide_gate", "tensor_core_gate"]
 # DRAM bytes (read + write) per amplitude of one stage-kernel launch, from the
 # ncu capture of the 26-qubit complex64 circuit on the packed-pair kernel
-# (537.16 MB read + 475.59 MB written per launch over 2^26 amplitudes);
+# (537.50 MB read + 475.22 MB written per launch over 2^26 amplitudes);
 # traffic grows with the state size, so a 30-qubit launch moves 2^30 times this.
-NCU_TRAFFIC_PER_AMP = {(1, 1): (537.16352e6 + 475.59424e6) / 2 ** 26}
+NCU_TRAFFIC_PER_AMP = {(1, 1): (537.502976e6 + 475.218944e6) / 2 ** 26}
 NCU_TRAFFIC_SOURCE = "profiles/stage_pk_kernel_c64_26q_ncu.md, scaled from 2^26 to 2^nq amplitudes"
 
 

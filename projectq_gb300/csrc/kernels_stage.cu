@@ -585,6 +585,44 @@ __device__ __forceinline__ void swap1(f2 (&RE)[16], f2 (&IM)[16], uint32_t amask
   }
 }
 
+__device__ __forceinline__ void xswap(f2 &a, f2 &b) {
+  asm("xor.b64 %0, %0, %1;\n\txor.b64 %1, %1, %0;\n\txor.b64 %0, %0, %1;" : "+l"(a), "+l"(b));
+}
+
+// X on register pair-bit B for the pairs whose register controls C (a
+// compile-time mask over the register index) are all set: a fixed register
+// swap of those pairs only, where swap1 selects over every pair.
+template <int B, int C>
+__device__ __forceinline__ void swapc(f2 (&RE)[16], f2 (&IM)[16]) {
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if (((j >> B) & 1) || (j & C) != C) continue;
+    const int k = j + (1 << B);
+    // in place (XOR exchange through PTX): each register keeps its
+    // allocation, where a renaming swap leaves the dispatch merge to move
+    // them back (ptxas: 1 KB of spills)
+    xswap(RE[j], RE[k]);
+    xswap(IM[j], IM[k]);
+  }
+}
+
+// Register-controlled X on bit B by its control mask: the eight subsets of
+// the other three register bits.
+template <int B>
+__device__ __forceinline__ void swap_ctl(f2 (&RE)[16], f2 (&IM)[16], uint32_t cmask) {
+  constexpr int O0 = B == 0 ? 2 : 1, O1 = B <= 1 ? 4 : 2, O2 = B <= 2 ? 8 : 4;  // the other bits
+  switch (cmask) {
+    case 0: swapc<B, 0>(RE, IM); break;
+    case O0: swapc<B, O0>(RE, IM); break;
+    case O1: swapc<B, O1>(RE, IM); break;
+    case O2: swapc<B, O2>(RE, IM); break;
+    case O0 | O1: swapc<B, O0 | O1>(RE, IM); break;
+    case O0 | O2: swapc<B, O0 | O2>(RE, IM); break;
+    case O1 | O2: swapc<B, O1 | O2>(RE, IM); break;
+    default: swapc<B, O0 | O1 | O2>(RE, IM); break;
+  }
+}
+
 // (RE, IM) *= F with F = Fx + i Fy per half: RE' = Fx RE - Fy IM, IM' = Fx IM + Fy RE
 __device__ __forceinline__ void cmul(f2 &re, f2 &im, f2 fx, f2 fy, f2 fn) {
   // both products first: each output's last instruction is then the last use
@@ -655,10 +693,10 @@ __device__ __forceinline__ void apply_op(f2 (&RE)[16], f2 (&IM)[16], const unsig
       case 1: dense1_cls<1>(RE, IM, M, op.amask, cls, masked); break;
       case 2: dense1_cls<2>(RE, IM, M, op.amask, cls, masked); break;
       case 3: dense1_cls<3>(RE, IM, M, op.amask, cls, masked); break;
-      case 4: swap1<0>(RE, IM, op.amask); break;
-      case 5: swap1<1>(RE, IM, op.amask); break;
-      case 6: swap1<2>(RE, IM, op.amask); break;
-      default: swap1<3>(RE, IM, op.amask); break;
+      case 4: swap_ctl<0>(RE, IM, cls); break;  // cls: the swap's register controls
+      case 5: swap_ctl<1>(RE, IM, cls); break;
+      case 6: swap_ctl<2>(RE, IM, cls); break;
+      default: swap_ctl<3>(RE, IM, cls); break;
     }
     return;
   }

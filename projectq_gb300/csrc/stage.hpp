@@ -393,7 +393,8 @@ constexpr uint32_t kPkCtl = 1u << 13;
 
 struct alignas(16) PkOpDev {
   uint32_t code;     // kind | b << 4 | cls << 8 | masked << 12 | kPkCtl (kPkDiagN: b is a pair-bit mask;
-                     // kPkLoadXor: the kind alone, its controls always tested)
+                     // kPkSwap: register controls in place of cls; kPkLoadXor: the kind alone, its controls
+                     // always tested)
   uint32_t data;     // blob offset of the operation's data (16-byte aligned)
   uint32_t amask;    // dense / swap with register controls: the register indices it pairs from (16 bits);
                      // folded X: the address XOR
@@ -617,7 +618,8 @@ inline bool build_substages_pk(StagePlan &sp) {
         for (uint32_t jj = 0; jj < 16; ++jj)
           if (!((jj >> bb) & 1) && (jj & jc) == jc) cd.d.amask |= 1u << jj;
         const uint32_t masked = jc ? 1u : 0u;
-        cd.d.code = (swap ? kPkSwap : kPkDense) | (bb << 4) | (cls << 8) | (masked << 12);
+        // swap: bits 8-11 carry its register controls (over the register index) instead of a class
+        cd.d.code = (swap ? kPkSwap : kPkDense) | (bb << 4) | ((swap ? jc : cls) << 8) | (masked << 12);
         cd.regs = (1u << bb) | jc;
         cd.swap = swap;
         cd.xor_type = swap && jc == 0;

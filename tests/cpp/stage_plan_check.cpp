@@ -272,8 +272,13 @@ void apply_stage_pk(std::vector<cplx> &psi, unsigned nq, const gsim::StagePlan &
               const bool rx = m[0].imag() == 0 && m[3].imag() == 0 && m[1].real() == 0 && m[2].real() == 0;
               const bool anti = m[0] == cplx(0.) && m[3] == cplx(0.);
               if ((cls == 1 && !real) || (cls == 2 && !rx) || (cls == 4 && !anti)) g_inconsistent = true;
-            } else if (!masked && (op.amask & 0xFFFFu) == 0) {
-              g_inconsistent = true;
+            } else {
+              if (!masked && (op.amask & 0xFFFFu) == 0) g_inconsistent = true;
+              // the kernel swaps the pairs of its register controls (code bits 8-11), not amask's
+              uint32_t want = 0;
+              for (uint32_t j = 0; j < 16; ++j)
+                if (!((j >> B) & 1) && (j & cls) == cls) want |= 1u << j;
+              if ((cls >> B) & 1 || want != (op.amask & 0xFFFFu) || masked != (cls != 0)) g_inconsistent = true;
             }
             for (uint32_t j = 0; j < 16; ++j) {
               if ((j >> B) & 1) continue;
