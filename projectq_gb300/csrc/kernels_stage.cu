@@ -567,31 +567,15 @@ __device__ __forceinline__ void dense1(f2 (&RE)[16], f2 (&IM)[16], const f2 *__r
   }
 }
 
-// X on register pair-bit B for the pairs in amask, as selects: the register
-// assignment stays fixed whatever the operation (a register renaming at a
-// run-time dispatch would need the same moves at every merge).
-template <int B>
-__device__ __forceinline__ void swap1(f2 (&RE)[16], f2 (&IM)[16], uint32_t amask) {
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    if ((j >> B) & 1) continue;
-    const int k = j + (1 << B);
-    const bool c = (amask >> j) & 1u;
-    const f2 r0 = RE[j], i0 = IM[j], r1 = RE[k], i1 = IM[k];
-    RE[j] = c ? r1 : r0;
-    IM[j] = c ? i1 : i0;
-    RE[k] = c ? r0 : r1;
-    IM[k] = c ? i0 : i1;
-  }
-}
-
+// a <-> b in place: three XORs through PTX, so both keep their registers
 __device__ __forceinline__ void xswap(f2 &a, f2 &b) {
   asm("xor.b64 %0, %0, %1;\n\txor.b64 %1, %1, %0;\n\txor.b64 %0, %0, %1;" : "+l"(a), "+l"(b));
 }
 
 // X on register pair-bit B for the pairs whose register controls C (a
-// compile-time mask over the register index) are all set: a fixed register
-// swap of those pairs only, where swap1 selects over every pair.
+// compile-time mask over the register index) are all set: a fixed exchange
+// of those pairs only (selects over every pair, with the mask at run time,
+// cost about 1.5x as many instructions).
 template <int B, int C>
 __device__ __forceinline__ void swapc(f2 (&RE)[16], f2 (&IM)[16]) {
 #pragma unroll
