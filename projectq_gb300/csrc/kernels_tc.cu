@@ -54,8 +54,9 @@ constexpr int kProducers = 256;    // warps 0-7
 constexpr int kEpilogue = 128;     // warps 8-11
 constexpr int kMmaWarp = 12;
 constexpr int kLoaderWarp = 13;
-constexpr int kPrefetch = 4;       // K-chunks of loads in flight per producer thread (6 measured slower:
-                                   // spills at k = 5 and no gain at k = 6, 7)
+constexpr int kPrefetch = 4;       // K-chunks of loads in flight per producer thread (5 measured slower,
+                                   // k = 5 gates 15.7 -> 18.4 ms at 32 qubits; 6: spills at k = 5 and no gain
+                                   // at k = 6, 7)
 constexpr uint32_t kStageA = uint32_t(kRows) * kKC * 4u;  // one split (hi or lo) of an A chunk
 
 template <int KQ>
