@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--fusion", default="staged", choices=["staged", "reference", "none"])
     ap.add_argument("--stage-kernel", default="packed", choices=["packed", "register", "pass"],
                     help="stage kernel of the staged planner (complex64 packed pairs by default)")
-    ap.add_argument("--c128-steps", type=int, default=None, help="timed steps of the complex128 arm")
+    ap.add_argument("--c128-steps", type=int, default=None,
+                    help="timed steps of the complex128 arm (default: --steps, at most 5: 5.5 s each at 30 qubits)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-gates", type=int, default=100, help="gates in each mode of the CPU baseline sample")
     ap.add_argument("--ref-gates", type=int, default=8,
@@ -870,7 +871,7 @@ def main():
     ms64 = allreduce_max(dist, ms64)
     key, groups = dominant_kernel(recs)
     # --- timed: complex128 -----------------------------------------------------
-    k128 = a.c128_steps if a.c128_steps is not None else max(1, a.steps)
+    k128 = a.c128_steps if a.c128_steps is not None else max(1, min(a.steps, 5))
     ms128, cnt128, _ = timed_steps(s128, gates, k128, max(1, min(a.warmup, 3)), dist, profile_kernel=False)
     ms128 = allreduce_max(dist, ms128)
     del s128
