@@ -453,3 +453,32 @@ def test_stage_kernels_against_oracle(n, mode):
     o.set_wavefunction(psi, list(range(n)))
     run_circuit(o, gates)
     assert np.max(np.abs(g.cheat()[1] - o.cheat()[1])) < 1e-5
+
+
+@pytest.mark.parametrize("n", [13, 16, 20])
+def test_packed_register_controlled_x_against_oracle(n):
+    """X gates with 0-3 controls all among four neighbouring qubits, between
+    rotations on them: inside a packed-pair substage these are in-place
+    exchanges of the pairs their register controls select (one body per
+    control mask), checked against the oracle (complex64, 1e-5)."""
+    rng = np.random.default_rng(100 + n)
+    from projectq_gb300.workloads import Rx, Ry, X
+    gates = []
+    for _ in range(120):
+        block = [int(q) for q in rng.permutation(4)] if rng.uniform() < 0.5 else [int(q) + 6 for q in rng.permutation(4)]
+        nctl = int(rng.integers(0, 4))
+        if rng.uniform() < 0.3:
+            gates.append(((Rx, Ry)[int(rng.integers(2))](float(rng.uniform(0, 2 * np.pi))), (block[0],), ()))
+        else:
+            gates.append((X, (block[0],), tuple(block[1:1 + nctl])))
+    psi = random_state(n, seed=n)
+    g = make("gpu", seed=1, precision="c64", fusion="staged")
+    g.set_stage_kernel("packed")
+    allocate(g, n)
+    g.set_wavefunction(psi.astype(np.complex64), list(range(n)))
+    run_circuit(g, gates)
+    o = make("oracle", seed=1)
+    allocate(o, n)
+    o.set_wavefunction(psi, list(range(n)))
+    run_circuit(o, gates)
+    assert np.max(np.abs(g.cheat()[1] - o.cheat()[1])) < 1e-5

@@ -186,6 +186,29 @@ def test_packed_pair_stages_equal_gate_by_gate(lib, n, seed, avoid, kind, dense2
         assert kinds[kind] >= 1, kinds
 
 
+@pytest.mark.parametrize("n", [13, 16])
+def test_packed_pair_register_controlled_x(lib, n):
+    """X gates with 0-3 controls among four neighbouring qubits, between
+    rotations on them: in a packed-pair substage each becomes the exchange of
+    the pairs its register controls select (the control mask travels in the
+    operation code; the emulator checks it against the pair mask).  Against
+    the oracle, tolerance 2e-6."""
+    rng = np.random.default_rng(200 + n)
+    from projectq_gb300.workloads import Rx, Ry, X
+    gates = []
+    for _ in range(60 if n > 13 else 30):
+        block = [int(q) for q in rng.permutation(4)] if rng.uniform() < 0.5 else [int(q) + 6 for q in rng.permutation(4)]
+        nctl = int(rng.integers(0, 4))
+        if rng.uniform() < 0.3:
+            gates.append(((Rx, Ry)[int(rng.integers(2))](float(rng.uniform(0, 2 * np.pi))), (block[0],), ()))
+        else:
+            gates.append((X, (block[0],), tuple(block[1:1 + nctl])))
+    psi = random_state(n, seed=n)
+    got, nst, npk, kinds = plan_apply_pk(lib, n, gates, psi)
+    assert npk >= 1
+    assert np.max(np.abs(got - oracle_apply(n, gates, psi))) < 2e-6
+
+
 def test_packed_pair_stage_with_pack_bit_above_the_runs(lib):
     """Dense gates only on qubits 0-9, diagonal gates and controls on every
     qubit but 18: each stage's dense targets leave room in the tile, and the
