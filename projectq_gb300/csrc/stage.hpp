@@ -438,42 +438,45 @@ inline bool build_substages_pk(StagePlan &sp) {
     }
     if ((ttouch[o] >> P) & 1) return false;  // the pack bit must be untouched
   }
-  std::vector<std::vector<size_t>> preds(nops);
+  // predecessors of each operation as a bitset over the operations
+  const size_t nwords = (nops + 63) / 64;
+  std::vector<uint64_t> predbits(nops * nwords, 0);
   for (size_t b = 0; b < nops; ++b)
     for (size_t a = 0; a < b; ++a)
       if (((ttouch[a] & ttouch[b]) || (gtouch[a] & gtouch[b])) && !(sp.ops[a].kind == 1 && sp.ops[b].kind == 1))
-        preds[b].push_back(a);
+        predbits[b * nwords + (a >> 6)] |= uint64_t(1) << (a & 63);
   struct Sub {
     std::vector<size_t> ops;
     uint32_t R;  // register tile bits (P included)
   };
   std::vector<Sub> subs;
-  std::vector<char> done(nops, 0);
+  std::vector<uint64_t> donebits(nwords, 0), trial(nwords, 0);
+  std::vector<size_t> memo(size_t(1) << L, 0);  // scheduled count per key, valid where memo_gen == gen
+  std::vector<uint32_t> memo_gen(size_t(1) << L, 0);
+  uint32_t gen = 0;
+  std::vector<uint32_t> cands4;  // the sets of 4 tile bits besides P, in increasing order
+  for (uint32_t cand = 0; cand < (1u << L); ++cand)
+    if (!((cand >> P) & 1) && __builtin_popcount(cand) == 4) cands4.push_back(cand);
   size_t ndone = 0;
   while (ndone < nops) {
     // The substage's register bits: of every set of 4 tile bits besides P,
     // the one under which list scheduling takes the most operations now
     // (ties: the first such set in enumeration order).
-    auto schedule = [&](uint32_t R, std::vector<char> &dn, std::vector<size_t> *chosen) {
+    // List scheduling under register bits R: every operation that is not yet
+    // done, fits R (dense ones: their target) and whose predecessors are all
+    // done.  Predecessors have lower indices, so one pass in index order
+    // reaches the fixed point.  Done sets are bitsets over the operations.
+    auto schedule = [&](uint32_t R, std::vector<uint64_t> &dn, std::vector<size_t> *chosen) {
       size_t taken = 0;
-      bool progress = true;
-      while (progress) {
-        progress = false;
-        for (size_t o = 0; o < nops; ++o) {
-          if (dn[o]) continue;
-          if (sp.ops[o].kind == 0 && (tmask[o] & ~R)) continue;
-          bool ready = true;
-          for (size_t p : preds[o])
-            if (!dn[p]) {
-              ready = false;
-              break;
-            }
-          if (!ready) continue;
-          dn[o] = 1;
-          ++taken;
-          if (chosen) chosen->push_back(o);
-          progress = true;
-        }
+      for (size_t o = 0; o < nops; ++o) {
+        if ((dn[o >> 6] >> (o & 63)) & 1) continue;
+        if (sp.ops[o].kind == 0 && (tmask[o] & ~R)) continue;
+        bool ready = true;
+        for (size_t w = 0; w < nwords && ready; ++w) ready = !(predbits[o * nwords + w] & ~dn[w]);
+        if (!ready) continue;
+        dn[o >> 6] |= uint64_t(1) << (o & 63);
+        ++taken;
+        if (chosen) chosen->push_back(o);
       }
       return taken;
     };
@@ -482,17 +485,27 @@ inline bool build_substages_pk(StagePlan &sp) {
     for (uint32_t b = 0, k = 0; b < L && k < 4; ++b)  // a valid set whatever happens below
       if (b != P) R |= 1u << b, ++k;
     R |= 1u << P;
-    for (uint32_t cand = 0; cand < (1u << L); ++cand) {
-      if (((cand >> P) & 1) || __builtin_popcount(cand) != 4) continue;
-      std::vector<char> dn = done;
-      const size_t taken = schedule(cand | (1u << P), dn, nullptr);
+    // the result depends on a set only through the target bits of the
+    // operations not yet done: each such intersection is scheduled once
+    uint32_t needed = 0;
+    for (size_t o = 0; o < nops; ++o)
+      if (sp.ops[o].kind == 0 && !((donebits[o >> 6] >> (o & 63)) & 1)) needed |= tmask[o];
+    ++gen;
+    for (uint32_t cand : cands4) {
+      const uint32_t key = cand & needed;
+      if (memo_gen[key] != gen) {
+        trial = donebits;
+        memo[key] = schedule(cand | (1u << P), trial, nullptr);
+        memo_gen[key] = gen;
+      }
+      const size_t taken = memo[key];
       if (taken > best_taken) {
         best_taken = taken;
         R = cand | (1u << P);
       }
     }
     std::vector<size_t> chosen;
-    ndone += schedule(R, done, &chosen);
+    ndone += schedule(R, donebits, &chosen);
     // pad to 5 register bits, from the bank classes (pair-bit mod 3) with most spare bits
     while (unsigned(__builtin_popcount(R)) < 5) {
       int best = -1, best_count = -1;
