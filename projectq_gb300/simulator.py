@@ -122,7 +122,7 @@ class Simulator:
         self._prec = _PRECISIONS[precision]
         h = C.c_void_p()
         self._check(self._api.create(int(rnd_seed), self._prec, C.byref(h)))
-        self._h = h
+        self.__dict__["_hv"] = h
         if fusion != "reference":
             self.set_fusion(fusion)
 
@@ -132,27 +132,29 @@ class Simulator:
 
     def close(self):
         """Free the engine's device memory now (the object is unusable after)."""
-        h = self.__dict__.get("_h")
+        h = self.__dict__.get("_hv")
         if h is not None and h.value:
             self._api.destroy(h)
-        self.__dict__["_h"] = None
+        self.__dict__["_hv"] = None
 
     def __del__(self):
         # Deferred: in a reference cycle (ProjectQ's MainEngine <-> backend)
         # Python may finalize this object before MainEngine.__del__ flushes
         # through it, as pybind11 objects are only freed after all finalizers.
         # The handle is destroyed at the next construction, close() or exit.
-        h = self.__dict__.get("_h")
+        h = self.__dict__.get("_hv")
         if h is not None and h.value:
             _PENDING.append((self._api, h))
 
-    def __getattribute__(self, name):
-        if name == "_h":
-            h = object.__getattribute__(self, "__dict__").get("_h")
-            if h is None:
-                raise RuntimeError("the simulator engine has been closed")
-            return h
-        return object.__getattribute__(self, name)
+    @property
+    def _h(self):
+        """The engine handle; a closed engine raises here.  (A property: a
+        __getattribute__ override would tax every attribute access of the
+        per-gate path.)"""
+        h = self.__dict__.get("_hv")
+        if h is None:
+            raise RuntimeError("the simulator engine has been closed")
+        return h
 
     @property
     def precision(self) -> str:
@@ -211,7 +213,7 @@ class Simulator:
             raise ValueError(f"apply_controlled_gate(): a {k}-qubit gate needs a {1 << k}x{1 << k} matrix")
         nc = len(ctrl)
         rc = self._api.apply_controlled_gate(self._h, mat.ctypes.data, k, (C.c_uint32 * k)(*ids),
-                                             (C.c_uint32 * nc)(*ctrl), nc)
+                                             (C.c_uint32 * nc)(*ctrl) if nc else None, nc)
         if rc:
             self._check(rc)
 
