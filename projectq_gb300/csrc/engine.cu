@@ -1453,6 +1453,12 @@ void Engine::execute_staged(std::vector<PlanStep> &steps, bool build) {
     StagePlan &sp = st.stage;
     if (build) build_stage_data(sp);
     const size_t o = off;
+    // this stage's bytes, checked against the staging buffer before any write
+    const size_t ops_bytes = !sp.pk.empty() ? round16(sp.pk.size())
+                             : !sp.subs.empty() ? stage_subs_bytes(sp) + round16(sp.sops.size() * sizeof(SubOpDev))
+                                                : round16(sp.ops.size() * sizeof(StageOpDev));
+    const size_t need = ops_bytes + (sp.pk.empty() ? round16(sp.pool.size() * esz) : 0);
+    if (o + need > bound) fail(GSIM_ERR_RUNTIME, "stage upload larger than its bound");
     size_t pool = 0;
     if (!sp.pk.empty()) {  // the packed-pair blob carries its own data
       std::memcpy(host + o, sp.pk.data(), sp.pk.size());
@@ -1479,7 +1485,6 @@ void Engine::execute_staged(std::vector<PlanStep> &steps, bool build) {
       }
       off += round16(sp.pool.size() * esz);
     }
-    if (off > bound) fail(GSIM_ERR_RUNTIME, "stage upload larger than its bound");
     CK(cudaMemcpyAsync(dev + o, host + o, off - o, cudaMemcpyHostToDevice, stream_));
     exec_stage(sp, dev + o, dev + pool);
   }
